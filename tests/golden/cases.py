@@ -1,0 +1,195 @@
+"""Parity cases shared by the golden-vector generator, the oracle tests and the GPU tests.
+
+Each case names: the mesh, how to build the operator from a torchfsm-like
+namespace (the reference package when generating fixtures, ``torchfsm_gb300``
+in the GPU tests), the same program in the oracle's vocabulary, the seeded
+initial condition, dt, the step count, the integrator and the recording
+interval. Sizes are small so that the FP64 oracle and the reference finish
+in seconds on a CPU.
+"""
+
+from __future__ import annotations
+
+import math
+from types import SimpleNamespace
+
+import numpy as np
+
+from torchfsm_gb300 import initial
+
+TWO_PI = 2.0 * math.pi
+
+
+def _sin_plus_half(mesh_info, batch, channels):
+    x = initial.mesh_points(mesh_info)[0]
+    return (np.sin(2.0 * np.pi * x) + 0.5).reshape(1, 1, -1).repeat(batch, 0)
+
+
+def _grf2(seed, n, batch=2):
+    return lambda mi, b, c: initial.gaussian_random_field((n, n), b, c, initial.vorticity_spectrum, seed)
+
+
+def _bl(seed, shape, kmax, rms):
+    return lambda mi, b, c: initial.band_limited(shape, b, c, kmax, seed, rms)
+
+
+def _grf3(seed, n):
+    return lambda mi, b, c: initial.gaussian_random_field((n, n, n), b, c, initial.velocity_spectrum, seed)
+
+
+def _kdv_ic(mesh_info, batch, channels):
+    x = initial.mesh_points(mesh_info)[0]
+    L = mesh_info[0][1] - mesh_info[0][0]
+    u = 0.5 * np.cos(2 * np.pi * x / L) + 0.3 * np.sin(4 * np.pi * x / L)
+    return u.reshape(1, 1, -1).repeat(batch, 0)
+
+
+def _kolmogorov_source(mesh_info, batch, channels):
+    # -4 cos(4 y) (forcing of the vorticity equation, sign as in field.kolm_force)
+    y = initial.mesh_points(mesh_info)[1]
+    f = -4.0 * np.cos(4.0 * y)
+    return np.broadcast_to(f.reshape(1, 1, 1, -1), (1, 1, mesh_info[0][2], mesh_info[1][2])).copy()
+
+
+CASES = {
+    # BASELINE configuration 1 exactly (README example).
+    "burgers1d_cfg1": dict(
+        mesh=[(0, 1, 128)], batch=1, channels=1, dt=0.01, step=200, record=1,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_sin_plus_half,
+    ),
+    # 2D vorticity NS, the cfg2 program on a small grid.
+    "ns2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=1, dt=0.01, step=50, record=10,
+        build=lambda M: M.pde.NavierStokesVorticity(1000),
+        lin=[(1.0 / 1000, ("laplacian",))], nl=[(-1.0, "vorticity_convection")],
+        ic=_grf2(11, 32),
+    ),
+    "ns2d_n64_re100": dict(
+        mesh=[(0, TWO_PI, 64), (0, TWO_PI, 64)], batch=1, channels=1, dt=0.005, step=40, record=0,
+        build=lambda M: M.pde.NavierStokesVorticity(100),
+        lin=[(1.0 / 100, ("laplacian",))], nl=[(-1.0, "vorticity_convection")],
+        ic=_grf2(12, 64),
+    ),
+    # 2D Burgers (two velocity channels).
+    "burgers2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=2, dt=0.01, step=40, record=10,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(21, (32, 32), 4, 0.25),
+    ),
+    "burgers2d_l1_n64": dict(
+        mesh=[(0, 1, 64), (0, 1, 64)], batch=1, channels=2, dt=0.001, step=30, record=0,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(22, (64, 64), 6, 0.5),
+    ),
+    # 1D Kuramoto-Sivashinsky on L = 32 pi (serving family).
+    "ks1d_n128": dict(
+        mesh=[(0, 32 * math.pi, 128)], batch=2, channels=1, dt=0.05, step=100, record=20,
+        build=lambda M: M.pde.KuramotoSivashinsky(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "convection")],
+        ic=_bl(31, (128,), 8, 1.0),
+    ),
+    # 1D Korteweg-de Vries: odd symbol (complex E, real-part phi quirk, complex Nyquist).
+    "kdv1d_n64": dict(
+        mesh=[(0, 20.0, 64)], batch=1, channels=1, dt=1e-3, step=100, record=25,
+        build=lambda M: M.pde.KortewegDeVries(),
+        lin=[(-1.0, ("spatial_derivative", 0, 3))], nl=[(6.0, "convection")],
+        ic=_kdv_ic,
+    ),
+    # 3D Burgers, three velocity channels.
+    "burgers3d_n16": dict(
+        mesh=[(0, TWO_PI, 16)] * 3, batch=1, channels=3, dt=0.01, step=10, record=0,
+        build=lambda M: M.pde.Burgers(0.005),
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_grf3(41, 16),
+    ),
+    # Linear-only program: the auto integrator is ETDRK0.
+    "heat2d_etdrk0": dict(
+        mesh=[(0, 1, 32), (0, 1, 32)], batch=2, channels=1, dt=0.001, step=10, record=1,
+        build=lambda M: 0.05 * M.operator.Laplacian(),
+        lin=[(0.05, ("laplacian",))], nl=[],
+        ic=_bl(51, (32, 32), 5, 1.0),
+    ),
+    # Batched viscosity: a [B,1,1] tensor coefficient.
+    "burgers1d_batched_nu": dict(
+        mesh=[(0, 1, 64)], batch=3, channels=1, dt=0.01, step=50, record=0,
+        build=lambda M: M.torch.tensor([0.01, 0.02, 0.05], dtype=M.torch.float64).reshape(3, 1, 1) * M.operator.Laplacian() - M.operator.Convection(),
+        lin=[(np.array([0.01, 0.02, 0.05]).reshape(3, 1, 1), ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(61, (64,), 5, 1.0),
+    ),
+    # High-dimensional KS: the mean removed is the mean over the whole batch.
+    "ksnd2d_n32": dict(
+        mesh=[(0, 10 * math.pi, 32), (0, 10 * math.pi, 32)], batch=2, channels=1, dt=0.05, step=20, record=5,
+        build=lambda M: M.pde.KuramotoSivashinskyHighDim(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")],
+        ic=_bl(71, (32, 32), 4, 0.5),
+    ),
+    # Velocity-form NS with the Leray projection.
+    "nsvel2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=1, channels=2, dt=0.01, step=20, record=0,
+        build=lambda M: M.pde.NavierStokes(100),
+        lin=[(1.0 / 100, ("laplacian",))], nl=[(1.0, "ns_pressure_convection")],
+        ic=_bl(81, (32, 32), 4, 0.5),
+    ),
+    # Vorticity NS with linear drag (unit implicit source) and an explicit Kolmogorov source.
+    "ns2d_kolmogorov_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=1, channels=1, dt=0.01, step=30, record=0,
+        build=lambda M: M.pde.NavierStokesVorticity(100) + (-0.1) * M.operator.ImplicitSource() - M.operator.ExplicitSource(M.torch.tensor(4.0 * np.cos(4.0 * initial.mesh_points([(0, TWO_PI, 32), (0, TWO_PI, 32)])[1])).reshape(1, 1, 1, 32).expand(1, 1, 32, 32)),
+        lin=[(1.0 / 100, ("laplacian",)), (-0.1, ("unit",))],
+        nl=[(-1.0, "vorticity_convection"), (-1.0, ("source_phys", 4.0))],
+        ic=_grf2(91, 32),
+    ),
+}
+
+# Alternative integrators on the cfg1 program (64 points, 50 steps).
+for _name in ("setdrk1", "setdrk2", "setdrk3", "etdrk1", "etdrk2"):
+    CASES[f"burgers1d_{_name}"] = dict(
+        mesh=[(0, 1, 64)], batch=1, channels=1, dt=0.005, step=50, record=0,
+        build=lambda M: M.pde.Burgers(0.02), integrator=_name,
+        lin=[(0.02, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_sin_plus_half,
+    )
+
+
+def initial_condition(name: str) -> np.ndarray:
+    c = CASES[name]
+    return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)
+
+
+def record_fn(name: str):
+    every = CASES[name]["record"]
+    if not every:
+        return None
+    return lambda step: step % every == 0
+
+
+def oracle_terms(name: str):
+    """Linear and nonlinear term lists in the oracle's vocabulary (sources resolved to spectra)."""
+    c = CASES[name]
+    nl = []
+    for coef, spec in c["nl"]:
+        if isinstance(spec, tuple) and spec[0] == "source_phys":
+            y = initial.mesh_points(c["mesh"])[1]
+            f = spec[1] * np.cos(spec[1] * y)
+            f = np.broadcast_to(f.reshape(1, 1, 1, -1), (1, 1, c["mesh"][0][2], c["mesh"][1][2]))
+            nl.append((coef, ("source", np.fft.fftn(f, axes=(-2, -1)))))
+        else:
+            nl.append((coef, spec))
+    return c["lin"], nl
+
+
+def namespace(module_root):
+    """torchfsm-like namespace (``pde``, ``operator``, ``torch``) from a package root module."""
+    import importlib
+    import torch
+
+    return SimpleNamespace(
+        pde=importlib.import_module(module_root + ".pde"),
+        operator=importlib.import_module(module_root + ".operator"),
+        integrator=importlib.import_module(module_root + ".integrator"),
+        traj_recorder=importlib.import_module(module_root + ".traj_recorder"),
+        torch=torch,
+    )

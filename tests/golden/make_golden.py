@@ -1,0 +1,121 @@
+"""Generate the golden vectors under tests/golden/ by running the reference.
+
+Run in a container where the reference (torchfsm 0.0.4) is importable:
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference is imported from the given source tree and run on the CPU in
+float64 for every case of ``cases.py``; the initial condition, the final
+physical state and (where recorded) the physical trajectory are stored in
+``<case>.npz``. ``phi_coefs.npz`` holds the reference's SETDRK4 / ETDRK
+coefficient tables for a few linear symbols and ``masks.npz`` its 2/3 dealias
+masks. These files are the pins of the numpy oracle and of the GPU path; the
+GPU machine never reads the reference itself.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+
+def main(ref_root: str) -> None:
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, REPO)
+    import torch
+
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+    import torchfsm  # noqa: F401  (the reference)
+    from torchfsm.integrator import ETDRKIntegrator, SETDRKIntegrator
+    from torchfsm.mesh import FourierMesh
+    from torchfsm.traj_recorder import AutoRecorder
+    from torchfsm.integrator._stable_etdrk._uncached import UnCachedSETDRK4, UnCachedSETDRK3
+    from torchfsm.integrator._etdrk import ETDRK2
+
+    sys.path.insert(0, HERE)
+    import cases as C
+
+    M = C.namespace("torchfsm")
+    enums = {
+        "setdrk1": SETDRKIntegrator.SETDRK1,
+        "setdrk2": SETDRKIntegrator.SETDRK2,
+        "setdrk3": SETDRKIntegrator.SETDRK3,
+        "setdrk4": SETDRKIntegrator.SETDRK4,
+        "etdrk0": ETDRKIntegrator.ETDRK0,
+        "etdrk1": ETDRKIntegrator.ETDRK1,
+        "etdrk2": ETDRKIntegrator.ETDRK2,
+    }
+    only = set(sys.argv[2:])
+    for name, case in C.CASES.items():
+        if only and name not in only:
+            continue
+        u0 = C.initial_condition(name)
+        op = case["build"](M)
+        if case.get("integrator"):
+            op.set_integrator(enums[case["integrator"]])
+        rec_fn = C.record_fn(name)
+        rec = AutoRecorder(control_func=rec_fn) if rec_fn is not None else None
+        out = op.integrate(
+            u_0=torch.tensor(u0, dtype=torch.float64),
+            mesh=case["mesh"],
+            dt=case["dt"],
+            step=case["step"],
+            trajectory_recorder=rec,
+        )
+        payload = {"u0": u0}
+        if rec is not None:
+            payload["traj"] = out.numpy()
+            payload["final"] = out[:, -1].numpy()
+        else:
+            payload["final"] = out.numpy()
+        payload["integrator"] = np.array(type(op._state_dict["integrator"]).__name__)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
+        print(name, payload["final"].shape, payload["integrator"])
+
+    if only:
+        return
+    # Coefficient tables (integrator/_stable_etdrk/_uncached.py:180-211, _etdrk.py:54-82).
+    tabs = {}
+    for tag, mesh_info, lin_fn, dt in (
+        ("ks1d", [(0, 32 * np.pi, 64)], lambda fm: -fm.laplacian() - fm.laplacian() ** 2, 0.1),
+        ("ns2d", [(0, 2 * np.pi, 32)] * 2, lambda fm: 1e-3 * fm.laplacian(), 1e-3),
+        ("kdv1d", [(0, 20.0, 64)], lambda fm: -fm.grad(0, 3), 1e-3),
+    ):
+        fm = FourierMesh(mesh_info, dtype=torch.float64)
+        L = lin_fn(fm)
+        tabs[f"{tag}_L"] = L.numpy()
+        for M_, r_ in ((16, 1.0), (32, 2.0)):
+            it = UnCachedSETDRK4(dt, L, None, M_, r_)
+            key = f"{tag}_m{M_}"
+            tabs[f"{key}_E"] = it._exp_term.numpy()
+            tabs[f"{key}_E2"] = it._half_exp_term.numpy()
+            for i in (1, 4, 5, 6):
+                tabs[f"{key}_c{i}"] = getattr(it, f"_coef_{i}").numpy()
+        it3 = UnCachedSETDRK3(dt, L, None, 16, 1.0)
+        for i in (1, 2, 3, 4, 5):
+            tabs[f"{tag}_s3_c{i}"] = getattr(it3, f"_coef_{i}").numpy()
+        e2 = ETDRK2(dt, L, None)
+        tabs[f"{tag}_e2_c1"] = e2._coef_1.numpy()
+        tabs[f"{tag}_e2_c2"] = e2._coef_2.numpy()
+        tabs[f"{tag}_dt"] = np.array(dt)
+    np.savez_compressed(os.path.join(HERE, "phi_coefs.npz"), **tabs)
+
+    # Dealias masks (mesh.py:443-461).
+    masks = {}
+    for n in (12, 16, 48, 96, 128, 256):
+        for dt_name, dtype in (("f32", torch.float32), ("f64", torch.float64)):
+            for rate in (2.0 / 3.0, 0.5, 1.0):
+                fm = FourierMesh([(0, 2 * np.pi, n)], dtype=dtype)
+                fm.set_default_rel_freq_threshold(rate)
+                masks[f"n{n}_{dt_name}_r{rate:.4f}"] = fm.low_pass_filter(rate).numpy().reshape(-1)
+    np.savez_compressed(os.path.join(HERE, "masks.npz"), **masks)
+    print("phi_coefs, masks written")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,149 @@
+/*
+ * torchfsm_gb300 C ABI: Fourier-spectral ETD time stepping on one GB300 (sm_103a).
+ *
+ * Plain C: every argument is a pointer, an integer, a double or a stream
+ * handle (cudaStream_t passed as void*). No C++ types or exceptions cross
+ * this boundary. Every entry point returns an FSM_* status; the message of
+ * the last failure on the calling host thread is read with fsm_last_error.
+ *
+ * Conventions
+ *  - Spectral fields are "half spectra": the transform over all spatial axes,
+ *    with the last axis kept for k = 0..n/2 only (the real-to-complex layout).
+ *    A field of a mesh (n0, .., n_{d-1}) holds S = n0*..*n_{d-2}*(n_{d-1}/2+1)
+ *    complex64 values, row-major; arrays are [batch][channel][S].
+ *  - The forward transform is unnormalised and the inverse carries 1/(n0*..)
+ *    (torch's "backward" norm), so half spectra equal the reference's
+ *    torch.fft.fftn output restricted to the last axis' first n/2+1 entries.
+ *  - Every buffer is allocated by the caller (device memory unless stated).
+ *    A plan owns only its constant tables (coefficients, wavenumbers, masks,
+ *    twiddles), is immutable after creation and may be used from several
+ *    host threads on different streams; workspaces are per call.
+ *  - All work is launched asynchronously on the given stream.
+ *  - Mesh sizes: powers of two, 16..4096 points in 1D, 16..512 per axis in
+ *    2D. Other programs/sizes return FSM_ERR_UNSUPPORTED.
+ *
+ * Reference interfaces replaced (torchfsm 0.0.4, paths in the torchfsm tree):
+ *  fsm_plan_create   OperatorLike._build_integrator / register_mesh linear-coefficient
+ *                    precompute: operator/_base.py:339-357, 441-526;
+ *                    UnCachedSETDRK1..4.__init__ integrator/_stable_etdrk/_uncached.py:46-211;
+ *                    ETDRK0..2.__init__ integrator/_etdrk.py:10-82
+ *  fsm_integrate     OperatorLike.integrate step loop operator/_base.py:726-746 with
+ *                    setdrk*_step integrator/_stable_etdrk/_setdrk_step.py:5-82, the
+ *                    nonlinear closure operator/_base.py:375-403 and the recorder
+ *                    traj_recorder.py:46-55
+ *  fsm_rfftn/irfftn  FourierMesh.fft / ifft(...).real mesh.py:481-491
+ */
+#ifndef TORCHFSM_GB300_H
+#define TORCHFSM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define FSM_OK 0
+#define FSM_ERR_INVALID 1      /* bad argument */
+#define FSM_ERR_UNSUPPORTED 2  /* program or size without a fused kernel */
+#define FSM_ERR_CUDA 3         /* a CUDA call failed */
+#define FSM_ERR_OOM 4          /* device allocation failed */
+#define FSM_ERR_NONFINITE 5    /* a result holds NaN or Inf */
+#define FSM_ERR_TIMEOUT 6      /* a bounded device wait ran out */
+
+/* nonlinear term of the program (at most one, plus an optional explicit source) */
+#define FSM_NL_NONE 0        /* linear, or explicit source only */
+#define FSM_NL_CONVECTION 1  /* (u.grad)u, C == ndim (operator/generic/_convection.py:18-46) */
+#define FSM_NL_VORTICITY 2   /* u.grad(w) with u from the streamfunction, 2D, C == 1
+                                (operator/dedicated/_navier_stokes.py:27-46) */
+#define FSM_NL_KS 3          /* 0.5 |grad phi|^2, C == 1 (operator/dedicated/_ks_convection.py:18-38) */
+#define FSM_NL_LERAY 4       /* -grad p - (u.grad)u, C == ndim (operator/dedicated/_navier_stokes.py:231-254) */
+
+/* program flags */
+#define FSM_FLAG_REMOVE_MEAN 1 /* FSM_NL_KS: subtract the mean over the whole batch */
+
+/* integrators (integrator/_etdrk.py, integrator/_stable_etdrk/) */
+#define FSM_ETDRK0 0
+#define FSM_ETDRK1 1
+#define FSM_ETDRK2 2
+#define FSM_SETDRK1 11
+#define FSM_SETDRK2 12
+#define FSM_SETDRK3 13
+#define FSM_SETDRK4 14
+
+typedef struct FsmPlan FsmPlan;
+
+typedef struct FsmMeshDesc {
+  int32_t ndim;      /* 1..3 */
+  int32_t n[3];      /* points per axis */
+  double length[3];  /* end - start per axis (mesh.py:185-191: f = fftfreq(n, length/n)) */
+} FsmMeshDesc;
+
+typedef struct FsmProgramDesc {
+  int32_t n_channel;
+  int32_t nonlinear;        /* FSM_NL_* */
+  int32_t flags;            /* FSM_FLAG_* */
+  int32_t integrator;       /* FSM_ETDRK* / FSM_SETDRK* */
+  double nonlinear_coef;    /* scalar coefficient of the nonlinear term */
+  const uint8_t* keep[3];   /* HOST: per axis, n[i] dealias keep flags in fftfreq order
+                               (mesh.py:443-461); NULL keeps every mode */
+  int32_t n_integration_points;  /* SETDRK contour points M (default 16) */
+  double integration_radius;     /* SETDRK contour radius r (default 1.0) */
+  const double* linear_coef;     /* DEVICE complex128 [lin_batch][lin_channel][S] (interleaved
+                                    re, im); NULL means L = 0 */
+  int32_t lin_batch;             /* 1 or the batch size */
+  int32_t lin_channel;           /* 1 or n_channel */
+  const void* source;            /* DEVICE complex64 [src_batch][n_channel][S], added to the
+                                    nonlinear value of every stage; NULL for none */
+  int32_t src_batch;             /* 1 or the batch size */
+} FsmProgramDesc;
+
+/* Build a plan: validates the program, copies the wavenumbers, masks and
+ * twiddles to the device and evaluates the exponential-integrator tables in
+ * FP64 on the device (contour-integral mean over M points for SETDRK), then
+ * rounds them to FP32. The linear coefficient buffer is read on `stream`
+ * and may be freed once the stream has passed this call. */
+int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* program, double dt, void* stream,
+                    FsmPlan** out);
+
+/* Release a plan (synchronises the device first). */
+int fsm_plan_destroy(FsmPlan* plan);
+
+/* Bytes of device workspace fsm_integrate needs for `batch` samples and `steps` steps. */
+int fsm_plan_workspace_bytes(const FsmPlan* plan, int32_t batch, int32_t steps, size_t* bytes);
+
+/* Number of kernel launches fsm_integrate makes for `steps` steps. */
+int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches);
+
+/* Advance `state` (half spectra, [batch][C][S] complex64, in place) by `steps`
+ * steps of dt. record_slot (HOST, steps+1 entries, or NULL): for step i
+ * (0 = initial state, steps = final state) the frame index in `traj` to
+ * write, or -1; traj is [batch][T][C][S] complex64 with T frames. */
+int fsm_integrate(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, const int32_t* record_slot,
+                  void* traj, int32_t n_frames, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Forward real transform over the plan's spatial axes: `count` real fields
+ * [count][n0..] (float32) -> half spectra [count][S] (complex64). */
+int fsm_rfftn(const FsmPlan* plan, int32_t count, const float* in, void* out, void* stream);
+
+/* Inverse: half spectra [count][S] -> real fields [count][n0..] with 1/N; the
+ * imaginary parts of self-conjugate modes are ignored (= ifftn(...).real).
+ * `in` is used as scratch and is overwritten. */
+int fsm_irfftn(const FsmPlan* plan, int32_t count, void* in, float* out, void* stream);
+
+/* Write, for each of `count` half-spectrum fields, 1 into flags[i] if it holds
+ * a NaN or Inf and 0 otherwise (device int32 array). */
+int fsm_nonfinite_flags(const FsmPlan* plan, int32_t count, const void* fields, int32_t* flags, void* stream);
+
+/* Copy the message of the last failure on this host thread into buf. */
+int fsm_last_error(char* buf, size_t len);
+
+/* ABI version of this library. */
+int fsm_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHFSM_GB300_H */

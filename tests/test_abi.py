@@ -1,0 +1,67 @@
+"""The C-ABI library builds for sm_103a, loads, and exports every symbol the header declares.
+
+No CUDA work is launched here (no GPU in the CPU suite).
+"""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from torchfsm_gb300 import _lib, build
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "torchfsm_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def libpath():
+    return build.build()
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(fsm_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_binding_exports():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(libpath):
+    out = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT\s+(fsm_\w+)", out))
+    missing = [f for f in declared_functions() if f not in exported]
+    assert not missing, missing
+
+
+def test_library_loads_and_reports_version(libpath):
+    lib = _lib.load(libpath)
+    assert lib.fsm_abi_version() == 1
+    buf = ctypes.create_string_buffer(64)
+    assert lib.fsm_last_error(buf, 64) == 0
+
+
+def test_invalid_arguments_return_status_without_gpu(libpath):
+    lib = _lib.load(libpath)
+    out = ctypes.c_void_p()
+    # null descriptors are rejected before any CUDA call
+    assert lib.fsm_plan_create(None, None, 0.1, None, ctypes.byref(out)) == _lib.FSM_ERR_INVALID
+    assert "null" in _lib.last_error()
+    mesh = _lib.FsmMeshDesc()
+    mesh.ndim = 1
+    mesh.n[0] = 100  # not a power of two
+    mesh.length[0] = 1.0
+    prog = _lib.FsmProgramDesc()
+    prog.n_channel = 1
+    prog.integrator = _lib.FSM_SETDRK4
+    prog.nonlinear = _lib.FSM_NL_CONVECTION
+    assert lib.fsm_plan_create(ctypes.byref(mesh), ctypes.byref(prog), 0.1, None, ctypes.byref(out)) == \
+        _lib.FSM_ERR_UNSUPPORTED
+    mesh.n[0] = 128
+    prog.nonlinear = _lib.FSM_NL_VORTICITY  # needs 2D
+    assert lib.fsm_plan_create(ctypes.byref(mesh), ctypes.byref(prog), 0.1, None, ctypes.byref(out)) == \
+        _lib.FSM_ERR_INVALID

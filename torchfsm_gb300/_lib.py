@@ -1,0 +1,141 @@
+"""ctypes binding of the C ABI in ``include/torchfsm_gb300.h``.
+
+The library is loaded on first use. When it is missing, or the tensors are
+not on a CUDA device, calls raise: there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from typing import Optional
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libtorchfsm_gb300.so")
+
+FSM_OK = 0
+FSM_ERR_INVALID = 1
+FSM_ERR_UNSUPPORTED = 2
+FSM_ERR_CUDA = 3
+FSM_ERR_OOM = 4
+FSM_ERR_NONFINITE = 5
+FSM_ERR_TIMEOUT = 6
+
+FSM_NL_NONE = 0
+FSM_NL_CONVECTION = 1
+FSM_NL_VORTICITY = 2
+FSM_NL_KS = 3
+FSM_NL_LERAY = 4
+
+FSM_FLAG_REMOVE_MEAN = 1
+
+FSM_ETDRK0 = 0
+FSM_ETDRK1 = 1
+FSM_ETDRK2 = 2
+FSM_SETDRK1 = 11
+FSM_SETDRK2 = 12
+FSM_SETDRK3 = 13
+FSM_SETDRK4 = 14
+
+# Every symbol the header declares; tests check that the library exports them.
+EXPORTS = (
+    "fsm_plan_create",
+    "fsm_plan_destroy",
+    "fsm_plan_workspace_bytes",
+    "fsm_plan_launch_count",
+    "fsm_integrate",
+    "fsm_rfftn",
+    "fsm_irfftn",
+    "fsm_nonfinite_flags",
+    "fsm_last_error",
+    "fsm_abi_version",
+)
+
+
+class FsmError(RuntimeError):
+    """A non-zero status from the library."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"torchfsm_gb300 error {code}: {message}")
+        self.code = code
+
+
+class UnsupportedProgram(FsmError):
+    """No fused kernel exists for this program or mesh."""
+
+
+class FsmMeshDesc(ctypes.Structure):
+    _fields_ = [("ndim", ctypes.c_int32), ("n", ctypes.c_int32 * 3), ("length", ctypes.c_double * 3)]
+
+
+class FsmProgramDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_channel", ctypes.c_int32),
+        ("nonlinear", ctypes.c_int32),
+        ("flags", ctypes.c_int32),
+        ("integrator", ctypes.c_int32),
+        ("nonlinear_coef", ctypes.c_double),
+        ("keep", ctypes.c_void_p * 3),
+        ("n_integration_points", ctypes.c_int32),
+        ("integration_radius", ctypes.c_double),
+        ("linear_coef", ctypes.c_void_p),
+        ("lin_batch", ctypes.c_int32),
+        ("lin_channel", ctypes.c_int32),
+        ("source", ctypes.c_void_p),
+        ("src_batch", ctypes.c_int32),
+    ]
+
+
+_lock = threading.Lock()
+_lib: Optional[ctypes.CDLL] = None
+
+
+def library_path() -> str:
+    return LIB_PATH
+
+
+def load(path: Optional[str] = None) -> ctypes.CDLL:
+    """Load (once) and return the library; raise if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"torchfsm_gb300 CUDA library not found at {p}; build it with "
+                "`python -m torchfsm_gb300.build` (nvcc, sm_103a)"
+            )
+        lib = ctypes.CDLL(p)
+        vp, i32, i64, sz = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_size_t
+        lib.fsm_plan_create.argtypes = [ctypes.POINTER(FsmMeshDesc), ctypes.POINTER(FsmProgramDesc), ctypes.c_double, vp,
+                                        ctypes.POINTER(vp)]
+        lib.fsm_plan_destroy.argtypes = [vp]
+        lib.fsm_plan_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
+        lib.fsm_plan_launch_count.argtypes = [vp, i32, ctypes.POINTER(i64)]
+        lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]
+        lib.fsm_rfftn.argtypes = [vp, i32, vp, vp, vp]
+        lib.fsm_irfftn.argtypes = [vp, i32, vp, vp, vp]
+        lib.fsm_nonfinite_flags.argtypes = [vp, i32, vp, vp, vp]
+        lib.fsm_last_error.argtypes = [ctypes.c_char_p, sz]
+        for name in EXPORTS:
+            getattr(lib, name).restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = ctypes.create_string_buffer(1024)
+    lib.fsm_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(code: int) -> None:
+    if code == FSM_OK:
+        return
+    msg = last_error()
+    if code == FSM_ERR_UNSUPPORTED:
+        raise UnsupportedProgram(code, msg)
+    raise FsmError(code, msg)

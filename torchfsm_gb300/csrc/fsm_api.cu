@@ -1,0 +1,512 @@
+// C ABI of torchfsm_gb300: plans, the FP64 coefficient kernel, the
+// integrate driver and the transforms. Declarations and the reference
+// interfaces each entry point replaces are in include/torchfsm_gb300.h.
+#include <math.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "fsm_internal.cuh"
+
+namespace fsm {
+
+static thread_local std::string g_last_error;
+
+int set_error(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return FSM_OK;
+  const int code = (e == cudaErrorMemoryAllocation) ? FSM_ERR_OOM : FSM_ERR_CUDA;
+  return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// FP64 coefficient tables
+// ---------------------------------------------------------------------------
+struct cd {
+  double x, y;
+};
+__device__ __forceinline__ cd mk(double x, double y) { return cd{x, y}; }
+__device__ __forceinline__ cd operator+(cd a, cd b) { return mk(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ cd operator-(cd a, cd b) { return mk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ cd operator*(cd a, cd b) { return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ cd operator*(double s, cd a) { return mk(s * a.x, s * a.y); }
+__device__ __forceinline__ cd operator+(double s, cd a) { return mk(s + a.x, a.y); }
+__device__ __forceinline__ cd cdiv(cd a, cd b) {
+  // Smith's algorithm (scaled by the larger component of b)
+  if (fabs(b.x) >= fabs(b.y)) {
+    const double r = b.y / b.x, den = b.x + b.y * r;
+    return mk((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  } else {
+    const double r = b.x / b.y, den = b.x * r + b.y;
+    return mk((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+  }
+}
+__device__ __forceinline__ cd cexpd(cd z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double e = exp(z.x);
+  return mk(e * c, e * s);
+}
+__device__ __forceinline__ float2 tof(cd z) { return make_float2((float)z.x, (float)z.y); }
+
+// One thread per (batch, channel, point) entry of L. Tables (float2) are
+// written at tab[t * ts + idx] in the scheme's order (fsm_common.cuh).
+// SETDRK: phi-functions as the mean over M contour points z_j = r e^{i pi (2j-1)/M} + dt L
+// of the Kassam-Trefethen integrands, real part kept (integrator/_stable_etdrk/_uncached.py:8-43, 46-211);
+// ETDRK1/2: closed forms with the L == 0 limits (integrator/_etdrk.py:30-82).
+__global__ void k_phi_tables(const double2* __restrict__ L, int64_t count, double dt, int integ, int M, double r,
+                             float2* __restrict__ tab, int64_t ts) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= count) return;
+  const cd l = L ? mk(L[idx].x, L[idx].y) : mk(0.0, 0.0);
+  const cd hl = dt * l;
+  const cd E = cexpd(hl);
+  tab[idx] = tof(E);
+  if (integ == FSM_ETDRK0) return;
+  if (integ == FSM_ETDRK1 || integ == FSM_ETDRK2) {
+    const bool zero = (l.x == 0.0 && l.y == 0.0);
+    const cd c1 = zero ? mk(dt, 0.0) : cdiv(E - mk(1.0, 0.0), l);
+    tab[ts + idx] = tof(c1);
+    if (integ == FSM_ETDRK2) {
+      const cd c2 = zero ? mk(0.5 * dt, 0.0) : cdiv(E - mk(1.0, 0.0) - hl, dt * (l * l));
+      tab[2 * ts + idx] = tof(c2);
+    }
+    return;
+  }
+  // contour sums
+  cd s_e1 = mk(0, 0), s_e2 = mk(0, 0), s_h = mk(0, 0), s_a = mk(0, 0), s_b = mk(0, 0), s_c = mk(0, 0);
+  for (int j = 1; j <= M; ++j) {
+    double sn, cs;
+    sincospi((double)(2 * j - 1) / (double)M, &sn, &cs);
+    const cd z = mk(r * cs, r * sn) + hl;
+    const cd ez = cexpd(z);
+    const cd z2 = z * z, z3 = z2 * z;
+    const cd one = mk(1.0, 0.0);
+    s_e1 = s_e1 + cdiv(ez - one, z);                                       // (e^z - 1)/z
+    s_e2 = s_e2 + cdiv(ez - one - z, z2);                                  // (e^z - 1 - z)/z^2
+    s_h = s_h + cdiv(cexpd(0.5 * z) - one, z);                             // (e^{z/2} - 1)/z
+    s_a = s_a + cdiv(mk(-4.0, 0.0) - z + ez * (mk(4.0, 0.0) - 3.0 * z + z2), z3);  // (-4 - z + e^z(4 - 3z + z^2))/z^3
+    s_b = s_b + cdiv(mk(2.0, 0.0) + z + ez * (mk(-2.0, 0.0) + z), z3);     // (2 + z + e^z(-2 + z))/z^3
+    s_c = s_c + cdiv(mk(-4.0, 0.0) - 3.0 * z - z2 + ez * (mk(4.0, 0.0) - z), z3);  // (-4 - 3z - z^2 + e^z(4 - z))/z^3
+  }
+  const double inv = dt / (double)M;
+  auto re = [&](cd s) { return make_float2((float)(inv * s.x), 0.f); };
+  switch (integ) {
+    case FSM_SETDRK1:
+      tab[ts + idx] = re(s_e1);
+      break;
+    case FSM_SETDRK2:
+      tab[ts + idx] = re(s_e1);
+      tab[2 * ts + idx] = re(s_e2);
+      break;
+    case FSM_SETDRK3:
+      tab[ts + idx] = tof(cexpd(0.5 * hl));
+      tab[2 * ts + idx] = re(s_h);
+      tab[3 * ts + idx] = re(s_e1);
+      tab[4 * ts + idx] = re(s_a);
+      tab[5 * ts + idx] = make_float2((float)(4.0 * inv * s_b.x), 0.f);
+      tab[6 * ts + idx] = re(s_c);
+      break;
+    case FSM_SETDRK4:
+    default:
+      tab[ts + idx] = tof(cexpd(0.5 * hl));
+      tab[2 * ts + idx] = re(s_h);
+      tab[3 * ts + idx] = re(s_a);
+      tab[4 * ts + idx] = re(s_b);
+      tab[5 * ts + idx] = re(s_c);
+      break;
+  }
+}
+
+// Linear programs (and explicit-source-only ones): the nonlinear value is the
+// constant source, so every point advances independently through all steps.
+__global__ void k_pointwise(StepArgs a, int64_t total) {
+  const int C = a.C;
+  const int64_t S = a.S;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s = idx % S;
+    const int c = (int)((idx / S) % C);
+    const int b = (int)(idx / (S * C));
+    float2 u = a.state[idx];
+    float2 acc = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
+    const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + s;
+    const float2* tab = a.tab + toff;
+    const float2 nv = a.src ? a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + s] : make_float2(0.f, 0.f);
+    const int slot0 = a.slots ? a.slots[0] : -1;
+    if (slot0 >= 0) a.traj[(((int64_t)b * a.n_frames + slot0) * C + c) * S + s] = u;
+    for (int step = 0; step < a.steps; ++step) {
+      if (a.integ == FSM_ETDRK0) {
+        u = cmul(tab[0], u);
+      } else {
+        for (int st = 0; st < a.nstages; ++st) (void)etd_stage(a.integ, st, nv, &u, &acc, &q, tab, a.ts);
+      }
+      const int slot = a.slots ? a.slots[step + 1] : -1;
+      if (slot >= 0) a.traj[(((int64_t)b * a.n_frames + slot) * C + c) * S + s] = u;
+    }
+    a.state[idx] = u;
+  }
+}
+
+int launch_pointwise(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  const int64_t total = (int64_t)a.B * a.C * a.S;
+  if (total == 0) return FSM_OK;
+  int blocks = (int)((total + 255) / 256);
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_pointwise<<<blocks, 256, 0, st>>>(a, total);
+  return cuda_check(cudaGetLastError(), "k_pointwise");
+}
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static void free_plan(FsmPlan* p) {
+  if (!p) return;
+  cudaFree(p->kvec);
+  cudaFree(p->keep);
+  cudaFree(p->tw);
+  cudaFree(p->tab);
+  cudaFree(p->source);
+  delete p;
+}
+
+}  // namespace fsm
+
+using namespace fsm;
+
+extern "C" {
+
+int fsm_abi_version(void) { return 1; }
+
+int fsm_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return FSM_ERR_INVALID;
+  strncpy(buf, g_last_error.c_str(), len - 1);
+  buf[len - 1] = '\0';
+  return FSM_OK;
+}
+
+int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double dt, void* stream, FsmPlan** out) {
+  if (!mesh || !prog || !out) return set_error(FSM_ERR_INVALID, "null argument");
+  *out = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nd = mesh->ndim;
+  if (nd < 1 || nd > 3) return set_error(FSM_ERR_INVALID, "ndim must be 1..3");
+  for (int i = 0; i < nd; ++i) {
+    const int n = mesh->n[i];
+    const int hi = (i == nd - 1) ? 4096 : 512;
+    if (!is_pow2(n) || n < 16 || n > hi)
+      return set_error(FSM_ERR_UNSUPPORTED, "axis " + std::to_string(i) + ": " + std::to_string(n) +
+                                                " points (need a power of two in 16.." + std::to_string(hi) + ")");
+    if (!(mesh->length[i] > 0.0)) return set_error(FSM_ERR_INVALID, "mesh length must be positive");
+  }
+  if (nd > 1 && mesh->n[nd - 1] > 512) return set_error(FSM_ERR_UNSUPPORTED, "multi-D last axis above 512 points");
+  const int C = prog->n_channel;
+  if (C < 1 || C > 8) return set_error(FSM_ERR_INVALID, "n_channel must be 1..8");
+  const int integ = prog->integrator;
+  if (scheme_tables(integ) == 0) return set_error(FSM_ERR_INVALID, "unknown integrator");
+  const int nl = prog->nonlinear;
+  int path = 0;
+  switch (nl) {
+    case FSM_NL_NONE:
+      path = 3;
+      break;
+    case FSM_NL_CONVECTION:
+      if (C != nd) return set_error(FSM_ERR_INVALID, "convection needs n_channel == ndim");
+      path = nd == 1 ? 1 : (nd == 2 ? 2 : 0);
+      break;
+    case FSM_NL_VORTICITY:
+      if (nd != 2 || C != 1) return set_error(FSM_ERR_INVALID, "vorticity convection needs a 2D scalar field");
+      path = 2;
+      break;
+    case FSM_NL_KS:
+      if (C != 1) return set_error(FSM_ERR_INVALID, "KS convection needs a scalar field");
+      path = nd == 1 ? 1 : (nd == 2 ? 2 : 0);
+      break;
+    case FSM_NL_LERAY:
+      if (C != nd) return set_error(FSM_ERR_INVALID, "Leray-projected convection needs n_channel == ndim");
+      path = nd == 2 ? 2 : 0;
+      break;
+    default:
+      return set_error(FSM_ERR_INVALID, "unknown nonlinear term");
+  }
+  if (path == 0) return set_error(FSM_ERR_UNSUPPORTED, "no fused kernel for this program on a " + std::to_string(nd) + "D mesh");
+  if (integ == FSM_ETDRK0 && (nl != FSM_NL_NONE || prog->source))
+    return set_error(FSM_ERR_INVALID, "ETDRK0 only supports linear programs");
+  if (nl == FSM_NL_NONE && integ != FSM_ETDRK0 && !prog->source && scheme_stages(integ) == 0)
+    return set_error(FSM_ERR_INVALID, "bad integrator");
+  if (prog->lin_batch < 1 || prog->lin_channel < 1 || (prog->lin_channel != 1 && prog->lin_channel != C))
+    return set_error(FSM_ERR_INVALID, "lin_batch/lin_channel");
+  if (prog->source && prog->src_batch < 1) return set_error(FSM_ERR_INVALID, "src_batch");
+  if (integ >= FSM_SETDRK1 && (prog->n_integration_points < 1 || !(prog->integration_radius > 0.0)))
+    return set_error(FSM_ERR_INVALID, "n_integration_points / integration_radius");
+
+  FsmPlan* p = new FsmPlan();
+  cudaGetDevice(&p->device);
+  p->ndim = nd;
+  for (int i = 0; i < 3; ++i) p->n[i] = i < nd ? mesh->n[i] : 1;
+  p->h = mesh->n[nd - 1] / 2 + 1;
+  p->S = p->h;
+  p->R = mesh->n[nd - 1];
+  for (int i = 0; i < nd - 1; ++i) {
+    p->S *= mesh->n[i];
+    p->R *= mesh->n[i];
+  }
+  p->C = C;
+  p->nl = nl;
+  p->flags = prog->flags;
+  p->integ = integ;
+  p->nstages = scheme_stages(integ);
+  p->ntab = scheme_tables(integ);
+  p->nl_coef = (float)prog->nonlinear_coef;
+  p->lin_batch = prog->linear_coef ? prog->lin_batch : 1;
+  p->lin_ch = prog->linear_coef ? prog->lin_channel : 1;
+  p->path = path;
+  p->n_aux = scheme_aux(integ);
+  if (path == 2) {
+    p->n_mid = (nl == FSM_NL_KS) ? 2 : 4;
+    p->n_prod = (nl == FSM_NL_CONVECTION || nl == FSM_NL_LERAY) ? 2 : 1;
+  }
+
+  int rc = FSM_OK;
+  // wavenumbers 2 pi f and keep flags per axis
+  int total_k = 0;
+  for (int i = 0; i < nd; ++i) {
+    p->koff[i] = total_k;
+    total_k += mesh->n[i];
+  }
+  std::vector<float> kv(total_k);
+  std::vector<uint8_t> keep(total_k, 1);
+  for (int i = 0; i < nd; ++i) {
+    const int n = mesh->n[i];
+    for (int j = 0; j < n; ++j) {
+      const int idx = (j < (n + 1) / 2) ? j : j - n;  // fftfreq ordering (n/2 -> -n/2)
+      kv[p->koff[i] + j] = (float)(2.0 * M_PI * (double)idx / mesh->length[i]);
+      if (prog->keep[i]) keep[p->koff[i] + j] = prog->keep[i][j] ? 1 : 0;
+    }
+  }
+  std::vector<float2> tw(kTwiddleMax);
+  for (int k = 0; k < kTwiddleMax; ++k) {
+    const double ang = 2.0 * M_PI * (double)k / (double)kTwiddleMax;
+    tw[k] = make_float2((float)cos(ang), (float)(-sin(ang)));
+  }
+  p->tstride = (int64_t)p->lin_batch * p->lin_ch * p->S;
+  const size_t tab_bytes = (size_t)p->ntab * p->tstride * sizeof(float2);
+  if ((rc = cuda_check(cudaMalloc(&p->kvec, total_k * sizeof(float)), "cudaMalloc kvec")) ||
+      (rc = cuda_check(cudaMalloc(&p->keep, total_k), "cudaMalloc keep")) ||
+      (rc = cuda_check(cudaMalloc(&p->tw, kTwiddleMax * sizeof(float2)), "cudaMalloc twiddles")) ||
+      (rc = cuda_check(cudaMalloc(&p->tab, tab_bytes), "cudaMalloc tables"))) {
+    free_plan(p);
+    return rc;
+  }
+  if ((rc = cuda_check(cudaMemcpyAsync(p->kvec, kv.data(), total_k * sizeof(float), cudaMemcpyHostToDevice, st), "copy kvec")) ||
+      (rc = cuda_check(cudaMemcpyAsync(p->keep, keep.data(), total_k, cudaMemcpyHostToDevice, st), "copy keep")) ||
+      (rc = cuda_check(cudaMemcpyAsync(p->tw, tw.data(), kTwiddleMax * sizeof(float2), cudaMemcpyHostToDevice, st), "copy twiddles"))) {
+    free_plan(p);
+    return rc;
+  }
+  if (prog->source) {
+    p->src_batch = prog->src_batch;
+    const size_t sb = (size_t)p->src_batch * C * p->S * sizeof(float2);
+    if ((rc = cuda_check(cudaMalloc(&p->source, sb), "cudaMalloc source")) ||
+        (rc = cuda_check(cudaMemcpyAsync(p->source, prog->source, sb, cudaMemcpyDeviceToDevice, st), "copy source"))) {
+      free_plan(p);
+      return rc;
+    }
+  }
+  const int64_t count = p->tstride;
+  const int threads = 128;
+  k_phi_tables<<<(unsigned)((count + threads - 1) / threads), threads, 0, st>>>(
+      (const double2*)prog->linear_coef, count, dt, integ,
+      prog->n_integration_points > 0 ? prog->n_integration_points : 16,
+      prog->integration_radius > 0 ? prog->integration_radius : 1.0, p->tab, p->tstride);
+  if ((rc = cuda_check(cudaGetLastError(), "k_phi_tables"))) {
+    free_plan(p);
+    return rc;
+  }
+  // The host vectors above are pageable: make sure the copies have consumed them.
+  if ((rc = cuda_check(cudaStreamSynchronize(st), "plan synchronise"))) {
+    free_plan(p);
+    return rc;
+  }
+  *out = p;
+  return FSM_OK;
+}
+
+int fsm_plan_destroy(FsmPlan* plan) {
+  if (!plan) return FSM_OK;
+  cudaDeviceSynchronize();
+  free_plan(plan);
+  return FSM_OK;
+}
+
+static size_t workspace_layout(const FsmPlan* p, int32_t batch, int32_t steps, size_t* off_arrays) {
+  size_t bytes = align256((size_t)(steps + 1) * sizeof(int32_t));  // record slots
+  bytes += 256;                                                    // KS batch-mean scratch
+  if (off_arrays) *off_arrays = bytes;
+  if (p->path == 2) {
+    const size_t per = (size_t)(p->n_aux * p->C + p->n_mid + p->n_prod) * p->S * sizeof(float2);
+    bytes += align256(per * (size_t)batch);
+  }
+  return bytes;
+}
+
+int fsm_plan_workspace_bytes(const FsmPlan* plan, int32_t batch, int32_t steps, size_t* bytes) {
+  if (!plan || !bytes || batch < 0 || steps < 0) return set_error(FSM_ERR_INVALID, "workspace_bytes arguments");
+  *bytes = workspace_layout(plan, batch, steps, nullptr);
+  return FSM_OK;
+}
+
+int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches) {
+  if (!plan || !launches || steps < 0) return set_error(FSM_ERR_INVALID, "launch_count arguments");
+  if (plan->path == 2) {
+    const int64_t per_stage = 2 + ((plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) ? 1 : 0);
+    *launches = 1 + (int64_t)steps * plan->nstages * per_stage;
+  } else {
+    *launches = 1;
+  }
+  return FSM_OK;
+}
+
+int fsm_integrate(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
+                  int32_t n_frames, void* workspace, size_t workspace_bytes, void* stream) {
+  if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
+  cudaStream_t st = (cudaStream_t)stream;
+  size_t off_arrays = 0;
+  const size_t need = workspace_layout(p, batch, steps, &off_arrays);
+  if (!workspace || workspace_bytes < need)
+    return set_error(FSM_ERR_INVALID, "workspace too small: need " + std::to_string(need) + " bytes");
+  if (p->lin_batch > 1 && p->lin_batch != batch) return set_error(FSM_ERR_INVALID, "batch != lin_batch");
+  if (p->source && p->src_batch > 1 && p->src_batch != batch) return set_error(FSM_ERR_INVALID, "batch != src_batch");
+  bool any_record = false;
+  if (record_slot) {
+    for (int i = 0; i <= steps; ++i) {
+      if (record_slot[i] >= n_frames) return set_error(FSM_ERR_INVALID, "record slot out of range");
+      any_record |= record_slot[i] >= 0;
+    }
+  }
+  if (any_record && !traj) return set_error(FSM_ERR_INVALID, "trajectory buffer missing");
+  if (p->path == 1 && p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN) && batch > 1)
+    return set_error(FSM_ERR_UNSUPPORTED, "1D KS mean removal over a batch > 1");
+
+  char* ws = (char*)workspace;
+  int32_t* d_slots = (int32_t*)ws;
+  int rc;
+  if (record_slot) {
+    if ((rc = cuda_check(cudaMemcpyAsync(d_slots, record_slot, (size_t)(steps + 1) * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, st), "copy record slots")))
+      return rc;
+  }
+  StepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.state = (float2*)state;
+  a.traj = (float2*)traj;
+  a.n_frames = n_frames;
+  a.slot = -1;
+  a.slots = record_slot ? d_slots : nullptr;
+  a.tab = p->tab;
+  a.ts = p->tstride;
+  a.lin_batch = p->lin_batch;
+  a.lin_ch = p->lin_ch;
+  a.src = p->source;
+  a.src_batch = p->src_batch;
+  a.kx = p->kvec + p->koff[0];
+  a.ky = p->kvec + p->koff[p->ndim - 1];
+  a.keepx = p->keep + p->koff[0];
+  a.keepy = p->keep + p->koff[p->ndim - 1];
+  a.tw = p->tw;
+  a.dc = (float2*)(ws + off_arrays - 256);
+  a.coef = p->nl_coef;
+  a.scale = (float)(1.0 / (double)p->R);
+  a.C = p->C;
+  a.n_aux = p->n_aux;
+  a.n_mid = p->n_mid;
+  a.n_prod = p->n_prod;
+  a.integ = p->integ;
+  a.nstages = p->nstages;
+  a.steps = steps;
+  a.B = batch;
+  a.flags = p->flags;
+  a.S = p->S;
+  a.H = p->h;
+
+  if (p->path == 3) return launch_pointwise(p, a, st);
+  if (p->path == 1) return launch_line(p, a, st);
+
+  // plane passes
+  float2* arr = (float2*)(ws + off_arrays);
+  const int64_t per_field = p->S;
+  a.aux = arr;
+  a.mid = a.aux + (int64_t)batch * p->n_aux * p->C * per_field;
+  a.prod = a.mid + (int64_t)batch * p->n_mid * per_field;
+  a.slots = nullptr;
+  const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
+  a.stage = -1;
+  a.emit = steps > 0;
+  a.slot = record_slot ? record_slot[0] : -1;
+  if ((rc = launch_plane_col(p, a, st))) return rc;
+  for (int step = 0; step < steps; ++step) {
+    for (int s = 0; s < p->nstages; ++s) {
+      if ((rc = launch_plane_row(p, a, st))) return rc;
+      if (ks_mean && (rc = launch_ks_mean(p, a, st))) return rc;
+      const bool last = s == p->nstages - 1;
+      a.stage = s;
+      a.emit = !(last && step == steps - 1);
+      a.slot = (last && record_slot) ? record_slot[step + 1] : -1;
+      if ((rc = launch_plane_col(p, a, st))) return rc;
+    }
+  }
+  return FSM_OK;
+}
+
+int fsm_rfftn(const FsmPlan* p, int32_t count, const float* in, void* out, void* stream) {
+  if (!p || !in || !out || count < 0) return set_error(FSM_ERR_INVALID, "rfftn arguments");
+  if (count == 0) return FSM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nd = p->ndim;
+  const int nl = p->n[nd - 1];
+  int64_t rows = (int64_t)count * (p->R / nl);
+  int rc = transform_r2c_last(nl, in, (float2*)out, rows, p->tw, st);
+  if (rc) return rc;
+  // outer axes, innermost first
+  int64_t inner = p->h;
+  for (int ax = nd - 2; ax >= 0; --ax) {
+    int64_t outer = count;
+    for (int j = 0; j < ax; ++j) outer *= p->n[j];
+    if (outer > 65535) return set_error(FSM_ERR_UNSUPPORTED, "rfftn: too many fields in one call");
+    if ((rc = transform_c2c_strided(p->n[ax], false, (float2*)out, outer, inner, p->tw, st))) return rc;
+    inner *= p->n[ax];
+  }
+  return FSM_OK;
+}
+
+int fsm_irfftn(const FsmPlan* p, int32_t count, void* in, float* out, void* stream) {
+  if (!p || !in || !out || count < 0) return set_error(FSM_ERR_INVALID, "irfftn arguments");
+  if (count == 0) return FSM_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nd = p->ndim;
+  int rc;
+  int64_t inner = p->h;
+  for (int ax = nd - 2; ax >= 0; --ax) {
+    int64_t outer = count;
+    for (int j = 0; j < ax; ++j) outer *= p->n[j];
+    if (outer > 65535) return set_error(FSM_ERR_UNSUPPORTED, "irfftn: too many fields in one call");
+    if ((rc = transform_c2c_strided(p->n[ax], true, (float2*)in, outer, inner, p->tw, st))) return rc;
+    inner *= p->n[ax];
+  }
+  const int nl = p->n[nd - 1];
+  const int64_t rows = (int64_t)count * (p->R / nl);
+  return transform_c2r_last(nl, (const float2*)in, out, rows, (float)(1.0 / (double)p->R), p->tw, st);
+}
+
+int fsm_nonfinite_flags(const FsmPlan* p, int32_t count, const void* fields, int32_t* flags, void* stream) {
+  if (!p || !fields || !flags || count < 0) return set_error(FSM_ERR_INVALID, "nonfinite arguments");
+  return launch_nonfinite((const float2*)fields, count, p->S, flags, (cudaStream_t)stream);
+}
+
+}  // extern "C"

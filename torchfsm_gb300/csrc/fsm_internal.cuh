@@ -1,0 +1,64 @@
+// Internal launchers shared between the torchfsm_gb300 CUDA sources.
+#pragma once
+
+#include "fsm_common.cuh"
+
+namespace fsm {
+
+// Arguments of the fused kernels that advance a batch of half spectra.
+struct StepArgs {
+  float2* state;              // [B][C][S]
+  float2* aux;                // [B][n_aux*C][S] scheme running sums (acc, q)
+  float2* mid;                // [B][n_mid][S]  stage fields after the outer-axis inverse transform
+  float2* prod;               // [B][n_prod][S] products after the last-axis forward transform
+  float2* traj;               // [B][n_frames][C][S]
+  int n_frames;
+  int slot;                   // frame written at the end of this launch, or -1
+  const int32_t* slots;       // device copy of the record slots (single-launch kernels)
+  const float2* tab;          // coefficient tables
+  int64_t ts;                 // distance between tables
+  int lin_batch, lin_ch;
+  const float2* src;          // explicit source or null
+  int src_batch;
+  const float* kx;            // 2 pi f of the first axis
+  const float* ky;            // 2 pi f of the last axis
+  const uint8_t* keepx;
+  const uint8_t* keepy;
+  const float2* tw;           // master twiddles
+  float2* dc;                 // batch-mean scratch of the KS mean removal
+  float coef;                 // nonlinear coefficient
+  float scale;                // 1 / (points per field)
+  int C, n_aux, n_mid, n_prod;
+  int integ, nstages;
+  int stage;                  // stage whose nonlinear value the launch consumes; -1 primes
+  int emit;                   // write the next stage's fields
+  int steps;
+  int B;
+  int flags;
+  int64_t S;
+  int H;
+};
+
+int transform_r2c_last(int n, const float* in, float2* out, int64_t rows, const float2* tw, cudaStream_t st);
+int transform_c2r_last(int n, const float2* in, float* out, int64_t rows, float scale, const float2* tw,
+                       cudaStream_t st);
+int transform_c2c_strided(int n, bool inverse, float2* data, int64_t outer, int64_t inner, const float2* tw,
+                          cudaStream_t st);
+int launch_nonfinite(const float2* f, int64_t count, int64_t S, int32_t* flags, cudaStream_t st);
+
+int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_ks_mean(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_pointwise(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+
+template <class K>
+inline int prep_smem(K kernel, size_t smem) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute");
+  }
+  return FSM_OK;
+}
+
+}  // namespace fsm

@@ -1,0 +1,132 @@
+// Fused 1D integration: one CTA per sample runs every step and stage of the
+// exponential Runge-Kutta scheme with the state, the scheme's running sums
+// and the transform buffer resident in shared memory, and writes recorded
+// frames straight into the trajectory. One launch per integrate call.
+//
+// Nonlinear terms (input dealiased, output not, operator/_base.py:375-403):
+//  FSM_NL_CONVECTION  u u_x: one inverse complex FFT of Z = D + i G with
+//                     D = mask*u_hat/N and G = i k D gives z = u + i u_x
+//                     (operator/generic/_convection.py:43-46);
+//  FSM_NL_KS          0.5 u_x^2 (operator/dedicated/_ks_convection.py:27-38).
+// followed by one forward FFT of the real product.
+#include "fsm_internal.cuh"
+
+namespace fsm {
+
+template <int N>
+struct LineCfg {
+  static constexpr int G = (N / 16 < 32) ? 32 : N / 16;
+  static constexpr bool BLOCK = G > 32;
+  static constexpr int H = N / 2 + 1;
+  static constexpr size_t SMEM = (size_t)(2 * N + 3 * H) * sizeof(float2);
+};
+
+// Build the inverse-transform input of the stage field `a` at index k.
+template <int N, int KIND>
+__device__ __forceinline__ void line_build(float2* __restrict__ Z, int k, float2 a, float keep, float kxv,
+                                           float scale) {
+  const float2 d = cscale(a, keep * scale);
+  float2 G = make_float2(-kxv * d.y, kxv * d.x);  // i k d
+  const bool selfc = (k == 0) || (k == N / 2);
+  if (KIND == FSM_NL_CONVECTION) {
+    float2 D = d;
+    if (selfc) {
+      D.y = 0.f;
+      G.y = 0.f;
+    }
+    Z[k] = make_float2(D.x - G.y, D.y + G.x);
+    if (!selfc) Z[N - k] = make_float2(D.x + G.y, G.x - D.y);
+  } else {  // FSM_NL_KS
+    if (selfc) G.y = 0.f;
+    Z[k] = G;
+    if (!selfc) Z[N - k] = cconj(G);
+  }
+}
+
+template <int N, int KIND>
+__global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
+  using Cfg = LineCfg<N>;
+  constexpr int H = Cfg::H;
+  constexpr int G = Cfg::G;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  float2* Z = tw + N;
+  float2* u = Z + N;
+  float2* acc = u + H;
+  float2* q = acc + H;
+  const int b = blockIdx.x;
+  const int t = threadIdx.x;
+  load_twiddles(tw, a.tw, kTwiddleMax, N, t, G);
+  float2* gstate = a.state + (int64_t)b * H;
+  for (int k = t; k < H; k += G) u[k] = gstate[k];
+  const int64_t toff = (int64_t)(a.lin_batch > 1 ? b : 0) * H;
+  const float2* tab = a.tab + toff;
+  const float2* src = a.src ? a.src + (int64_t)(a.src_batch > 1 ? b : 0) * H : nullptr;
+  const int slot0 = a.slots ? a.slots[0] : -1;
+  for (int k = t; k < H; k += G) {
+    if (slot0 >= 0) a.traj[((int64_t)b * a.n_frames + slot0) * H + k] = u[k];
+    if (a.steps > 0) line_build<N, KIND>(Z, k, u[k], (float)a.keepx[k], a.kx[k], a.scale);
+  }
+  __syncthreads();
+  const int ns = a.nstages;
+  for (int step = 0; step < a.steps; ++step) {
+    for (int s = 0; s < ns; ++s) {
+      fft<N, G, Cfg::BLOCK, true>(Z, tw, t);
+      for (int n = t; n < N; n += G) {
+        const float2 z = Z[n];
+        const float p = (KIND == FSM_NL_CONVECTION) ? z.x * z.y : 0.5f * z.x * z.x;
+        Z[n] = make_float2(p, 0.f);
+      }
+      __syncthreads();
+      fft<N, G, Cfg::BLOCK, false>(Z, tw, t);
+      const bool last = (s == ns - 1);
+      const bool final_stage = last && (step == a.steps - 1);
+      const int slot = (last && a.slots) ? a.slots[step + 1] : -1;
+      for (int k = t; k < H; k += G) {
+        float2 nv = cscale(Z[k], a.coef);
+        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && k == 0) nv = make_float2(0.f, 0.f);
+        if (src) nv = cadd(nv, src[k]);
+        const float2 nxt = etd_stage(a.integ, s, nv, u + k, acc + k, q + k, tab + k, a.ts);
+        if (!final_stage) line_build<N, KIND>(Z, k, nxt, (float)a.keepx[k], a.kx[k], a.scale);
+        if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H + k] = u[k];
+      }
+      __syncthreads();
+    }
+  }
+  for (int k = t; k < H; k += G) gstate[k] = u[k];
+}
+
+template <int N, int KIND>
+static int launch_line_n(const StepArgs& a, cudaStream_t st) {
+  using Cfg = LineCfg<N>;
+  int rc = prep_smem(k_line<N, KIND>, Cfg::SMEM);
+  if (rc) return rc;
+  k_line<N, KIND><<<a.B, Cfg::G, Cfg::SMEM, st>>>(a);
+  return cuda_check(cudaGetLastError(), "k_line");
+}
+
+template <int KIND>
+static int launch_line_kind(int n, const StepArgs& a, cudaStream_t st) {
+  switch (n) {
+    case 16: return launch_line_n<16, KIND>(a, st);
+    case 32: return launch_line_n<32, KIND>(a, st);
+    case 64: return launch_line_n<64, KIND>(a, st);
+    case 128: return launch_line_n<128, KIND>(a, st);
+    case 256: return launch_line_n<256, KIND>(a, st);
+    case 512: return launch_line_n<512, KIND>(a, st);
+    case 1024: return launch_line_n<1024, KIND>(a, st);
+    case 2048: return launch_line_n<2048, KIND>(a, st);
+    case 4096: return launch_line_n<4096, KIND>(a, st);
+  }
+  return set_error(FSM_ERR_UNSUPPORTED, "1D: unsupported length " + std::to_string(n));
+}
+
+int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  switch (p->nl) {
+    case FSM_NL_CONVECTION: return launch_line_kind<FSM_NL_CONVECTION>(p->n[0], a, st);
+    case FSM_NL_KS: return launch_line_kind<FSM_NL_KS>(p->n[0], a, st);
+  }
+  return set_error(FSM_ERR_UNSUPPORTED, "1D: unsupported nonlinear term");
+}
+
+}  // namespace fsm

@@ -1,0 +1,3 @@
+from ._convection import ConservativeConvection, Convection
+from ._linear import Biharmonic, Laplacian, SpatialDerivative
+from ._source import ImplicitSource

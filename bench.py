@@ -268,6 +268,24 @@ def row_pass_bytes(B: int) -> float:
     return 5.0 * 8.0 * B * N * H
 
 
+def ncu_case():
+    """Full batch (inputs larger than L2), 3 SETDRK4 steps: 25 launches after a 9-launch warm-up."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    entry.build()
+    from torchfsm_gb300 import pde
+
+    device = torch.device("cuda", 0)
+    u = torch.tensor(initial_vorticity(BATCH), device=device)
+    op = pde.NavierStokesVorticity(RE)
+    op.integrate(u_0=u, mesh=MESH, dt=DT, step=1)
+    out = op.integrate(u_0=u, dt=DT, step=3)
+    torch.cuda.synchronize()
+    print("ncu case done", bool(torch.isfinite(out).all().item()))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -276,7 +294,12 @@ def main():
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=16)
     ap.add_argument("--cpu-time-steps", type=int, default=5)
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="small profiling case: one warm-up step, then 3 time steps of the full batch")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case()
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     threads = os.cpu_count() or 1

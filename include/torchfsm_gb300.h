@@ -123,6 +123,15 @@ int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches)
 int fsm_integrate(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, const int32_t* record_slot,
                   void* traj, int32_t n_frames, void* workspace, size_t workspace_bytes, void* stream);
 
+/* fsm_integrate without recording, with every kernel launch bracketed by CUDA
+ * events on `stream`; blocks until the work is done. kernel_ms[4] and
+ * kernel_launches[4] (HOST) receive the summed device time and the launch
+ * count per kernel kind: 0 column pass, 1 row pass, 2 first column pass
+ * (priming), 3 other (1D line, pointwise, batch means). Instrumentation for
+ * benchmarks; not for production loops. */
+int fsm_integrate_profiled(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, void* workspace,
+                           size_t workspace_bytes, void* stream, double* kernel_ms, int64_t* kernel_launches);
+
 /* Forward real transform over the plan's spatial axes: `count` real fields
  * [count][n0..] (float32) -> half spectra [count][S] (complex64). */
 int fsm_rfftn(const FsmPlan* plan, int32_t count, const float* in, void* out, void* stream);

@@ -45,6 +45,7 @@ EXPORTS = (
     "fsm_plan_workspace_bytes",
     "fsm_plan_launch_count",
     "fsm_integrate",
+    "fsm_integrate_profiled",
     "fsm_rfftn",
     "fsm_irfftn",
     "fsm_nonfinite_flags",
@@ -115,6 +116,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_plan_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
         lib.fsm_plan_launch_count.argtypes = [vp, i32, ctypes.POINTER(i64)]
         lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]
+        lib.fsm_integrate_profiled.argtypes = [vp, i32, vp, i32, vp, sz, vp, ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(i64)]
         lib.fsm_rfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_irfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_nonfinite_flags.argtypes = [vp, i32, vp, vp, vp]

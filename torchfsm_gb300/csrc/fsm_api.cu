@@ -373,16 +373,67 @@ int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches)
   return FSM_OK;
 }
 
-int fsm_integrate(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
-                  int32_t n_frames, void* workspace, size_t workspace_bytes, void* stream) {
+}  // extern "C"
+
+namespace {
+
+// Optional per-launch CUDA-event timing (fsm_integrate_profiled).
+struct LaunchProfile {
+  std::vector<cudaEvent_t> start, stop;
+  std::vector<int> kind;
+  cudaStream_t st;
+  int begin(int k) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return FSM_ERR_CUDA;
+    cudaEventRecord(e, st);
+    start.push_back(e);
+    kind.push_back(k);
+    return FSM_OK;
+  }
+  int end() {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return FSM_ERR_CUDA;
+    cudaEventRecord(e, st);
+    stop.push_back(e);
+    return FSM_OK;
+  }
+  int collect(double* ms, int64_t* count) {
+    if (!stop.empty()) {
+      cudaError_t err = cudaEventSynchronize(stop.back());
+      if (err != cudaSuccess) return cuda_check(err, "profile synchronise");
+    }
+    for (size_t i = 0; i < stop.size(); ++i) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, start[i], stop[i]);
+      ms[kind[i]] += t;
+      count[kind[i]] += 1;
+    }
+    for (auto e : start) cudaEventDestroy(e);
+    for (auto e : stop) cudaEventDestroy(e);
+    return FSM_OK;
+  }
+};
+
+enum { kProfColumn = 0, kProfRow = 1, kProfPrime = 2, kProfOther = 3 };
+
+template <class F>
+int timed(LaunchProfile* prof, int kind, F&& launch) {
+  if (prof) prof->begin(kind);
+  int rc = launch();
+  if (prof) prof->end();
+  return rc;
+}
+
+int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
+                   int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof) {
   if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
-  cudaStream_t st = (cudaStream_t)stream;
   size_t off_arrays = 0;
   const size_t need = workspace_layout(p, batch, steps, &off_arrays);
   if (!workspace || workspace_bytes < need)
     return set_error(FSM_ERR_INVALID, "workspace too small: need " + std::to_string(need) + " bytes");
   if (p->lin_batch > 1 && p->lin_batch != batch) return set_error(FSM_ERR_INVALID, "batch != lin_batch");
   if (p->source && p->src_batch > 1 && p->src_batch != batch) return set_error(FSM_ERR_INVALID, "batch != src_batch");
+  if ((int64_t)batch * p->C > 65535 && p->path == 2) return set_error(FSM_ERR_UNSUPPORTED, "batch too large for one launch");
   bool any_record = false;
   if (record_slot) {
     for (int i = 0; i <= steps; ++i) {
@@ -435,8 +486,8 @@ int fsm_integrate(const FsmPlan* p, int32_t batch, void* state, int32_t steps, c
   a.S = p->S;
   a.H = p->h;
 
-  if (p->path == 3) return launch_pointwise(p, a, st);
-  if (p->path == 1) return launch_line(p, a, st);
+  if (p->path == 3) return timed(prof, kProfOther, [&] { return launch_pointwise(p, a, st); });
+  if (p->path == 1) return timed(prof, kProfOther, [&] { return launch_line(p, a, st); });
 
   // plane passes
   float2* arr = (float2*)(ws + off_arrays);
@@ -449,19 +500,43 @@ int fsm_integrate(const FsmPlan* p, int32_t batch, void* state, int32_t steps, c
   a.stage = -1;
   a.emit = steps > 0;
   a.slot = record_slot ? record_slot[0] : -1;
-  if ((rc = launch_plane_col(p, a, st))) return rc;
+  if ((rc = timed(prof, kProfPrime, [&] { return launch_plane_col(p, a, st); }))) return rc;
   for (int step = 0; step < steps; ++step) {
     for (int s = 0; s < p->nstages; ++s) {
-      if ((rc = launch_plane_row(p, a, st))) return rc;
-      if (ks_mean && (rc = launch_ks_mean(p, a, st))) return rc;
+      if ((rc = timed(prof, kProfRow, [&] { return launch_plane_row(p, a, st); }))) return rc;
+      if (ks_mean && (rc = timed(prof, kProfOther, [&] { return launch_ks_mean(p, a, st); }))) return rc;
       const bool last = s == p->nstages - 1;
       a.stage = s;
       a.emit = !(last && step == steps - 1);
       a.slot = (last && record_slot) ? record_slot[step + 1] : -1;
-      if ((rc = launch_plane_col(p, a, st))) return rc;
+      if ((rc = timed(prof, kProfColumn, [&] { return launch_plane_col(p, a, st); }))) return rc;
     }
   }
   return FSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsm_integrate(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
+                  int32_t n_frames, void* workspace, size_t workspace_bytes, void* stream) {
+  return integrate_impl(p, batch, state, steps, record_slot, traj, n_frames, workspace, workspace_bytes,
+                        (cudaStream_t)stream, nullptr);
+}
+
+int fsm_integrate_profiled(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
+                           size_t workspace_bytes, void* stream, double* kernel_ms, int64_t* kernel_launches) {
+  if (!kernel_ms || !kernel_launches) return set_error(FSM_ERR_INVALID, "profile outputs");
+  for (int i = 0; i < 4; ++i) {
+    kernel_ms[i] = 0.0;
+    kernel_launches[i] = 0;
+  }
+  LaunchProfile prof;
+  prof.st = (cudaStream_t)stream;
+  int rc = integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, prof.st, &prof);
+  int rc2 = prof.collect(kernel_ms, kernel_launches);
+  return rc ? rc : rc2;
 }
 
 int fsm_rfftn(const FsmPlan* p, int32_t count, const float* in, void* out, void* stream) {

@@ -132,6 +132,23 @@ int fsm_integrate(const FsmPlan* plan, int32_t batch, void* state, int32_t steps
 int fsm_integrate_profiled(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, void* workspace,
                            size_t workspace_bytes, void* stream, double* kernel_ms, int64_t* kernel_launches);
 
+/* Size of the device scratch array behind fsm_integrate_static (32 MiB per GPU). */
+#define FSM_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* fsm_integrate (no recording) for callers that cannot allocate device memory:
+ * code that may not call cudaMalloc or an allocating library after start-up
+ * (host callbacks, allocation-free plugin hosts, real-time loops). Its scratch
+ * is a fixed FSM_STATIC_SCRATCH_BYTES device array inside this library, held
+ * by every GPU that loads it until the process exits; the caller still passes
+ * the plan (created beforehand; plan creation allocates) and the state. Work
+ * whose scratch would exceed the array (fsm_plan_workspace_bytes) is rejected
+ * with FSM_ERR_INVALID. The first call on a device looks up the array's device
+ * address and must come before any stream capture on that device. All calls
+ * share the one array: calls that overlap on the GPU (other streams, other
+ * threads) race and corrupt each other's results; serialise them. No
+ * counterpart in the reference. */
+int fsm_integrate_static(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, void* stream);
+
 /* Forward real transform over the plan's spatial axes: `count` real fields
  * [count][n0..] (float32) -> half spectra [count][S] (complex64). */
 int fsm_rfftn(const FsmPlan* plan, int32_t count, const float* in, void* out, void* stream);

@@ -30,6 +30,8 @@ FSM_NL_LERAY = 4
 
 FSM_FLAG_REMOVE_MEAN = 1
 
+FSM_STATIC_SCRATCH_BYTES = 32 * 1024 * 1024  # include/torchfsm_gb300.h
+
 FSM_ETDRK0 = 0
 FSM_ETDRK1 = 1
 FSM_ETDRK2 = 2
@@ -46,6 +48,7 @@ EXPORTS = (
     "fsm_plan_launch_count",
     "fsm_integrate",
     "fsm_integrate_profiled",
+    "fsm_integrate_static",
     "fsm_rfftn",
     "fsm_irfftn",
     "fsm_nonfinite_flags",
@@ -118,6 +121,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]
         lib.fsm_integrate_profiled.argtypes = [vp, i32, vp, i32, vp, sz, vp, ctypes.POINTER(ctypes.c_double),
                                                ctypes.POINTER(i64)]
+        lib.fsm_integrate_static.argtypes = [vp, i32, vp, i32, vp]
         lib.fsm_rfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_irfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_nonfinite_flags.argtypes = [vp, i32, vp, vp, vp]

@@ -424,6 +424,16 @@ int timed(LaunchProfile* prof, int kind, F&& launch) {
   return rc;
 }
 
+}  // namespace
+
+namespace fsm {
+size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps) {
+  return workspace_layout(p, batch, steps, nullptr);
+}
+}  // namespace fsm
+
+namespace {
+
 int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
                    int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof) {
   if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
@@ -516,6 +526,13 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
 }
 
 }  // namespace
+
+namespace fsm {
+int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
+                             size_t workspace_bytes, cudaStream_t st) {
+  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr);
+}
+}  // namespace fsm
 
 extern "C" {
 

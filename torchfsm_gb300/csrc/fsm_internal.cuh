@@ -46,6 +46,11 @@ int transform_c2c_strided(int n, bool inverse, float2* data, int64_t outer, int6
                           cudaStream_t st);
 int launch_nonfinite(const float2* f, int64_t count, int64_t S, int32_t* flags, cudaStream_t st);
 
+// fsm_integrate without recording on a caller-provided workspace (fsm_api.cu).
+int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
+                             size_t workspace_bytes, cudaStream_t st);
+size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps);
+
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st);

@@ -52,6 +52,9 @@ int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32
 size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps);
 
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+// Register-FFT plane passes (64..256 points per axis); return -1 when no kernel covers the sizes.
+int launch_plane_col_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_plane_row_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_ks_mean(const FsmPlan* p, const StepArgs& a, cudaStream_t st);

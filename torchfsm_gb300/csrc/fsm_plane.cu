@@ -331,6 +331,8 @@ static int row_dispatch(int nx, int ny, const StepArgs& a, cudaStream_t st) {
 }
 
 int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  const int r = launch_plane_col_reg(p, a, st);
+  if (r != -1) return r;
   switch (p->nl) {
     case FSM_NL_VORTICITY: return col_dispatch<FSM_NL_VORTICITY>(p->n[0], a, st);
     case FSM_NL_CONVECTION: return col_dispatch<FSM_NL_CONVECTION>(p->n[0], a, st);
@@ -341,6 +343,8 @@ int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
 }
 
 int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  const int r = launch_plane_row_reg(p, a, st);
+  if (r != -1) return r;
   switch (p->nl) {
     case FSM_NL_VORTICITY: return row_dispatch<FSM_NL_VORTICITY>(p->n[0], p->n[1], a, st);
     case FSM_NL_CONVECTION:

@@ -1,0 +1,385 @@
+// Register-FFT versions of the 2D column and row passes (64..256 points per
+// axis). Same arithmetic and layout as fsm_plane.cu; the transforms run in
+// registers (fsm_regfft.cuh) so each 1D transform touches shared memory once
+// (the pass-1/pass-2 transpose) instead of once per Stockham pass.
+//
+// Row pass: a group of T lanes owns a pair of rows. It loads the mid fields
+// straight from global memory into the transform layout (the Hermitian
+// extension k > NY/2 comes from the mirrored entry), runs the inverse
+// transforms, forms the physical product in registers, runs the forward
+// transform of the two rows' products packed as one complex row and splits
+// the half spectra with one shuffle per output register.
+//
+// Column pass: a CTA owns W = 256/T adjacent ky columns of one sample. The
+// products are staged into a padded column-major tile (coalesced loads), each
+// group transforms one column, the stage update runs with a coalesced point
+// mapping, and each next-stage field is transformed per column and staged
+// through a second tile for coalesced stores.
+#include "fsm_internal.cuh"
+#include "fsm_regfft.cuh"
+
+namespace fsm {
+
+template <int KIND>
+struct RegKind {
+  static constexpr int C = (KIND == FSM_NL_CONVECTION || KIND == FSM_NL_LERAY) ? 2 : 1;
+  static constexpr int NM = (KIND == FSM_NL_KS) ? 2 : 4;
+};
+
+template <int NX>
+struct ColCfg {
+  using RS = RegShape<NX>;
+  static constexpr int T = RS::T;
+  static constexpr int E = RS::E;
+  static constexpr int W = 256 / T;
+  static constexpr int NEED = (NX > E * (T + 1)) ? NX : E * (T + 1);
+  static constexpr int P = NEED | 1;  // odd pitch: a row across W columns hits W distinct banks
+};
+
+template <int NX, int KIND>
+__global__ void __launch_bounds__(256) k_plane_col_r(StepArgs a) {
+  using Cfg = ColCfg<NX>;
+  using K = RegKind<KIND>;
+  constexpr int T = Cfg::T, E = Cfg::E, W = Cfg::W, P = Cfg::P, C = K::C;
+  extern __shared__ float2 smem[];
+  float2* twt = smem;                   // NX
+  float2* tileA = smem + NX;            // C * W * P: products -> N -> next stage field
+  float2* tileB = tileA + C * W * P;    // W * P: transpose scratch and output staging
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int b = blockIdx.y;
+  const int c0 = blockIdx.x * W;
+  const int H = a.H;
+  const int64_t S = a.S;
+  load_reg_twiddles<NX>(twt, a.tw, threadIdx.x, 256);
+
+  if (a.stage >= 0) {
+    for (int f = 0; f < C; ++f) {
+      const float2* src = a.prod + ((int64_t)b * a.n_prod + f) * S;
+      for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+        const int row = idx / W, col = idx % W;
+        if (c0 + col < H) tileA[(f * W + col) * P + row] = src[(int64_t)row * H + c0 + col];
+      }
+    }
+    __syncthreads();
+    for (int f = 0; f < C; ++f) {
+      float2* colp = tileA + (f * W + g) * P;
+      float2 v[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) v[j] = colp[t + T * j];
+      reg_fft<NX, false>(v, tileB + g * P, twt, t);
+#pragma unroll
+      for (int j = 0; j < E; ++j) colp[t + T * j] = v[j];
+    }
+  }
+  __syncthreads();
+
+  const bool last = a.stage == a.nstages - 1;
+  for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+    const int row = idx / W, col = idx % W;
+    const int ky_i = c0 + col;
+    if (ky_i >= H) continue;
+    const int64_t sidx = (int64_t)row * H + ky_i;
+    float2 nv[C];
+    if (a.stage >= 0) {
+#pragma unroll
+      for (int c = 0; c < C; ++c) nv[c] = tileA[(c * W + col) * P + row];
+      if (KIND == FSM_NL_LERAY) {
+        const float kxv = a.kx[row], kyv = a.ky[ky_i];
+        const float lap = -(kxv * kxv + kyv * kyv);
+        const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+        const float2 div = cadd(cscale(cmuli(nv[0]), kxv), cscale(cmuli(nv[1]), kyv));
+        const float2 pr = cscale(div, il);
+        const float2 n0 = csub(cscale(cmuli(pr), kxv), nv[0]);
+        const float2 n1 = csub(cscale(cmuli(pr), kyv), nv[1]);
+        nv[0] = n0;
+        nv[1] = n1;
+      }
+      if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && ky_i == 0) nv[0] = csub(nv[0], a.dc[0]);
+#pragma unroll
+      for (int c = 0; c < C; ++c) {
+        nv[c] = cscale(nv[c], a.coef);
+        if (a.src) nv[c] = cadd(nv[c], a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
+      }
+    }
+    const float m = (float)(a.keepx[row] & a.keepy[ky_i]) * a.scale;
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+      float2* up = a.state + ((int64_t)b * C + c) * S + sidx;
+      float2 st;
+      if (a.stage < 0) {
+        st = *up;
+      } else {
+        float2* accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
+        float2* qp = a.aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
+        const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+        st = etd_stage(a.integ, a.stage, nv[c], up, accp, qp, a.tab + toff, a.ts);
+      }
+      if (a.slot >= 0 && (a.stage < 0 || last)) a.traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
+      tileA[(c * W + col) * P + row] = cscale(st, m);
+    }
+  }
+  if (!a.emit) return;
+  __syncthreads();
+
+  const int col = c0 + g;
+  const float kyv = a.ky[col < H ? col : H - 1];
+  float kxr[E];
+#pragma unroll
+  for (int j = 0; j < E; ++j) kxr[j] = a.kx[t + T * j];
+  for (int mf = 0; mf < K::NM; ++mf) {
+    const int c = (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) ? 0 : (mf >> 1);
+    const float2* colp = tileA + (c * W + g) * P;
+    float2 v[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float2 d = colp[t + T * j];
+      const float kxv = kxr[j];
+      float2 x;
+      if (KIND == FSM_NL_VORTICITY) {
+        // 0: psi = -w/lap, 1: i kx psi, 2: w, 3: i kx w
+        if (mf < 2) {
+          const float lap = -(kxv * kxv + kyv * kyv);
+          const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+          const float2 psi = cscale(d, -il);
+          x = (mf == 0) ? psi : cscale(cmuli(psi), kxv);
+        } else {
+          x = (mf == 2) ? d : cscale(cmuli(d), kxv);
+        }
+      } else {
+        // KS: 0: phi, 1: i kx phi; convection: 2c: u_c, 2c+1: i kx u_c
+        x = (mf & 1) ? cscale(cmuli(d), kxv) : d;
+      }
+      v[j] = x;
+    }
+    float2* ob = tileB + g * P;
+    reg_fft<NX, true>(v, ob, twt, t);
+#pragma unroll
+    for (int j = 0; j < E; ++j) ob[t + T * j] = v[j];
+    __syncthreads();
+    float2* dst = a.mid + ((int64_t)b * a.n_mid + mf) * S;
+    for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+      const int row = idx / W, cc = idx % W;
+      if (c0 + cc < H) dst[(int64_t)row * H + c0 + cc] = tileB[cc * P + row];
+    }
+    __syncthreads();
+  }
+}
+
+template <int NY>
+struct RowCfgR {
+  using RS = RegShape<NY>;
+  static constexpr int T = RS::T;
+  static constexpr int E = RS::E;
+  static constexpr int SCR = reg_scratch<NY>();
+};
+
+__device__ __forceinline__ float2 herm_z(float2 A, float2 B, bool selfc, bool hi) {
+  if (selfc) {
+    A.y = 0.f;
+    B.y = 0.f;
+  }
+  if (hi) {
+    A.y = -A.y;
+    B.y = -B.y;
+  }
+  return make_float2(A.x - B.y, A.y + B.x);  // A + i B
+}
+
+// Split the transform of p0 + i p1 (lane t holds K = t + T j in register j)
+// into the half spectra of p0 and p1 and store k = 0..NY/2.
+template <int NY>
+__device__ __forceinline__ void split_store_r(const float2 (&zp)[RegShape<NY>::E], int t, int lane,
+                                              float2* __restrict__ out0, float2* __restrict__ out1) {
+  constexpr int T = RegShape<NY>::T, E = RegShape<NY>::E;
+  constexpr int J = NY / (2 * T);
+  const int partner_lane = (lane & ~(T - 1)) | ((T - t) & (T - 1));
+#pragma unroll
+  for (int j = 0; j <= J; ++j) {
+    const float2 send = zp[E - 1 - j];
+    float2 recv;
+    recv.x = __shfl_sync(0xffffffffu, send.x, partner_lane);
+    recv.y = __shfl_sync(0xffffffffu, send.y, partner_lane);
+    const float2 partner = (t == 0) ? zp[(E - j) & (E - 1)] : recv;
+    const int k = t + T * j;
+    if (k <= NY / 2) {
+      const float2 zm = cconj(partner);
+      out0[k] = cscale(cadd(zp[j], zm), 0.5f);
+      out1[k] = cscale(cmulmi(csub(zp[j], zm)), 0.5f);
+    }
+  }
+}
+
+template <int NY, int KIND>
+__global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
+  using Cfg = RowCfgR<NY>;
+  constexpr int T = Cfg::T, E = Cfg::E, SCR = Cfg::SCR;
+  constexpr int H = NY / 2 + 1;
+  extern __shared__ float2 smem[];
+  float2* twt = smem;
+  const int lane = threadIdx.x & 31;
+  const int g = threadIdx.x / T, t = threadIdx.x % T;
+  const int groups = blockDim.x / T;
+  float2* scr = smem + NY + g * SCR;
+  load_reg_twiddles<NY>(twt, a.tw, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const int b = blockIdx.y;
+  const int r0 = (blockIdx.x * groups + g) * 2;
+  const int64_t S = a.S;
+  const float* ky = a.ky;
+  const float2* mid = a.mid + (int64_t)b * a.n_mid * S;
+  float2* prod = a.prod + (int64_t)b * a.n_prod * S;
+
+  if (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) {
+    float p[2][E];
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr) {
+      const int64_t roff = (int64_t)(r0 + rr) * H;
+      float2 Z1[E], Z2[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const int k = t + T * j;
+        const bool hi = k > NY / 2;
+        const int kk = hi ? NY - k : k;
+        const bool selfc = (kk == 0) || (kk == NY / 2);
+        const float kyv = ky[kk];
+        if (KIND == FSM_NL_VORTICITY) {
+          const float2 m0 = mid[roff + kk], m1 = mid[S + roff + kk];
+          const float2 m2 = mid[2 * S + roff + kk], m3 = mid[3 * S + roff + kk];
+          // u_x + i u_y with u_x <- i ky psi, u_y <- -(i kx psi); w_x + i w_y with w_x <- i kx w, w_y <- i ky w
+          Z1[j] = herm_z(cscale(cmuli(m0), kyv), make_float2(-m1.x, -m1.y), selfc, hi);
+          Z2[j] = herm_z(m3, cscale(cmuli(m2), kyv), selfc, hi);
+        } else {
+          const float2 m0 = mid[roff + kk], m1 = mid[S + roff + kk];
+          Z1[j] = herm_z(m1, cscale(cmuli(m0), kyv), selfc, hi);  // phi_x + i phi_y
+        }
+      }
+      reg_fft<NY, true>(Z1, scr, twt, t);
+      if (KIND == FSM_NL_VORTICITY) {
+        reg_fft<NY, true>(Z2, scr, twt, t);
+#pragma unroll
+        for (int j = 0; j < E; ++j) p[rr][j] = Z1[j].x * Z2[j].x + Z1[j].y * Z2[j].y;
+      } else {
+#pragma unroll
+        for (int j = 0; j < E; ++j) p[rr][j] = 0.5f * (Z1[j].x * Z1[j].x + Z1[j].y * Z1[j].y);
+      }
+    }
+    float2 zp[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) zp[j] = make_float2(p[0][j], p[1][j]);
+    reg_fft<NY, false>(zp, scr, twt, t);
+    split_store_r<NY>(zp, t, lane, prod + (int64_t)r0 * H, prod + (int64_t)(r0 + 1) * H);
+  } else {
+    // convection, C = 2: conv_c = u0 dx u_c + u1 dy u_c
+#pragma unroll 1
+    for (int rr = 0; rr < 2; ++rr) {
+      const int64_t roff = (int64_t)(r0 + rr) * H;
+      float2 Z1[E], Z2[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const int k = t + T * j;
+        const bool hi = k > NY / 2;
+        const int kk = hi ? NY - k : k;
+        const bool selfc = (kk == 0) || (kk == NY / 2);
+        Z1[j] = herm_z(mid[roff + kk], mid[2 * S + roff + kk], selfc, hi);          // u0 + i u1
+        Z2[j] = herm_z(mid[S + roff + kk], mid[3 * S + roff + kk], selfc, hi);      // dx u0 + i dx u1
+      }
+      reg_fft<NY, true>(Z1, scr, twt, t);
+      reg_fft<NY, true>(Z2, scr, twt, t);
+      float2 acc[E];
+      float u1[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        acc[j] = make_float2(Z1[j].x * Z2[j].x, Z1[j].x * Z2[j].y);
+        u1[j] = Z1[j].y;
+      }
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const int k = t + T * j;
+        const bool hi = k > NY / 2;
+        const int kk = hi ? NY - k : k;
+        const bool selfc = (kk == 0) || (kk == NY / 2);
+        const float kyv = ky[kk];
+        Z2[j] = herm_z(cscale(cmuli(mid[roff + kk]), kyv), cscale(cmuli(mid[2 * S + roff + kk]), kyv), selfc, hi);
+      }
+      reg_fft<NY, true>(Z2, scr, twt, t);  // dy u0 + i dy u1
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        acc[j].x += u1[j] * Z2[j].x;
+        acc[j].y += u1[j] * Z2[j].y;
+      }
+      reg_fft<NY, false>(acc, scr, twt, t);
+      split_store_r<NY>(acc, t, lane, prod + roff, prod + S + roff);
+    }
+  }
+}
+
+template <int NX, int KIND>
+static int launch_col_r(const StepArgs& a, cudaStream_t st) {
+  using Cfg = ColCfg<NX>;
+  using K = RegKind<KIND>;
+  const size_t smem = (size_t)(NX + (K::C + 1) * Cfg::W * Cfg::P) * sizeof(float2);
+  int rc = prep_smem(k_plane_col_r<NX, KIND>, smem);
+  if (rc) return rc;
+  dim3 grid((a.H + Cfg::W - 1) / Cfg::W, a.B);
+  k_plane_col_r<NX, KIND><<<grid, 256, smem, st>>>(a);
+  return cuda_check(cudaGetLastError(), "k_plane_col_r");
+}
+
+template <int NY, int KIND>
+static int launch_row_r(int nx, const StepArgs& a, cudaStream_t st) {
+  using Cfg = RowCfgR<NY>;
+  const int groups_needed = nx / 2;
+  int threads = groups_needed * Cfg::T;
+  if (threads > 256) threads = 256;
+  const int groups = threads / Cfg::T;
+  const size_t smem = (size_t)(NY + groups * Cfg::SCR) * sizeof(float2);
+  int rc = prep_smem(k_plane_row_r<NY, KIND>, smem);
+  if (rc) return rc;
+  dim3 grid(groups_needed / groups, a.B);
+  k_plane_row_r<NY, KIND><<<grid, threads, smem, st>>>(a);
+  return cuda_check(cudaGetLastError(), "k_plane_row_r");
+}
+
+template <int KIND>
+static int col_r_dispatch(int nx, const StepArgs& a, cudaStream_t st) {
+  switch (nx) {
+    case 64: return launch_col_r<64, KIND>(a, st);
+    case 128: return launch_col_r<128, KIND>(a, st);
+    case 256: return launch_col_r<256, KIND>(a, st);
+  }
+  return -1;
+}
+
+template <int KIND>
+static int row_r_dispatch(int nx, int ny, const StepArgs& a, cudaStream_t st) {
+  if (nx < 2) return -1;
+  switch (ny) {
+    case 64: return launch_row_r<64, KIND>(nx, a, st);
+    case 128: return launch_row_r<128, KIND>(nx, a, st);
+    case 256: return launch_row_r<256, KIND>(nx, a, st);
+  }
+  return -1;
+}
+
+// Returns -1 when no register-FFT kernel exists for the sizes (caller falls back).
+int launch_plane_col_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  switch (p->nl) {
+    case FSM_NL_VORTICITY: return col_r_dispatch<FSM_NL_VORTICITY>(p->n[0], a, st);
+    case FSM_NL_CONVECTION: return col_r_dispatch<FSM_NL_CONVECTION>(p->n[0], a, st);
+    case FSM_NL_LERAY: return col_r_dispatch<FSM_NL_LERAY>(p->n[0], a, st);
+    case FSM_NL_KS: return col_r_dispatch<FSM_NL_KS>(p->n[0], a, st);
+  }
+  return -1;
+}
+
+int launch_plane_row_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  switch (p->nl) {
+    case FSM_NL_VORTICITY: return row_r_dispatch<FSM_NL_VORTICITY>(p->n[0], p->n[1], a, st);
+    case FSM_NL_CONVECTION:
+    case FSM_NL_LERAY: return row_r_dispatch<FSM_NL_CONVECTION>(p->n[0], p->n[1], a, st);
+    case FSM_NL_KS: return row_r_dispatch<FSM_NL_KS>(p->n[0], p->n[1], a, st);
+  }
+  return -1;
+}
+
+}  // namespace fsm

@@ -144,6 +144,44 @@ CASES = {
     ),
 }
 
+CASES.update({
+    # 3D high-dimensional KS (scalar, batch-wide mean removal).
+    "ksnd3d_n16": dict(
+        mesh=[(0, 10 * math.pi, 16)] * 3, batch=2, channels=1, dt=0.05, step=10, record=0,
+        build=lambda M: M.pde.KuramotoSivashinskyHighDim(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")],
+        ic=_bl(101, (16, 16, 16), 3, 0.5),
+    ),
+    # 3D velocity Navier-Stokes with the Leray projection.
+    "nsvel3d_n16": dict(
+        mesh=[(0, TWO_PI, 16)] * 3, batch=1, channels=3, dt=0.01, step=10, record=5,
+        build=lambda M: M.pde.NavierStokes(100),
+        lin=[(1.0 / 100, ("laplacian",))], nl=[(1.0, "ns_pressure_convection")],
+        ic=_bl(111, (16, 16, 16), 3, 0.5),
+    ),
+    # 3D Burgers on 32^3, two samples.
+    "burgers3d_n32": dict(
+        mesh=[(0, TWO_PI, 32)] * 3, batch=2, channels=3, dt=0.005, step=8, record=0,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_grf3(121, 32),
+    ),
+    # 2D vorticity NS on 512^2 (the largest 2D size).
+    "ns2d_n512": dict(
+        mesh=[(0, TWO_PI, 512), (0, TWO_PI, 512)], batch=1, channels=1, dt=1e-3, step=4, record=0,
+        build=lambda M: M.pde.NavierStokesVorticity(1000),
+        lin=[(1.0 / 1000, ("laplacian",))], nl=[(-1.0, "vorticity_convection")],
+        ic=_grf2(131, 512),
+    ),
+    # 2D Burgers at the differentiable workload's size (128^2, two channels).
+    "burgers2d_n128": dict(
+        mesh=[(0, TWO_PI, 128), (0, TWO_PI, 128)], batch=2, channels=2, dt=0.005, step=20, record=0,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(141, (128, 128), 6, 1.0),
+    ),
+})
+
 # Alternative integrators on the cfg1 program (64 points, 50 steps).
 for _name in ("setdrk1", "setdrk2", "setdrk3", "etdrk1", "etdrk2"):
     CASES[f"burgers1d_{_name}"] = dict(

@@ -67,12 +67,17 @@ def main(ref_root: str) -> None:
             step=case["step"],
             trajectory_recorder=rec,
         )
-        payload = {"u0": u0}
+        # Large arrays are stored in float32 (6e-8 relative, far inside the 1e-5 parity bar)
+        # and large initial conditions not at all (they are regenerated from their seed).
+        def small(x):
+            return x if x.size <= 131072 else x.astype(np.float32)
+
+        payload = {"u0": u0} if u0.size <= 65536 else {}
         if rec is not None:
-            payload["traj"] = out.numpy()
-            payload["final"] = out[:, -1].numpy()
+            payload["traj"] = small(out.numpy())
+            payload["final"] = small(out[:, -1].numpy())
         else:
-            payload["final"] = out.numpy()
+            payload["final"] = small(out.numpy())
         payload["integrator"] = np.array(type(op._state_dict["integrator"]).__name__)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
         print(name, payload["final"].shape, payload["integrator"])

@@ -20,7 +20,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 TOL = 1e-5
 pytestmark = pytest.mark.gpu
 
-SUPPORTED = [n for n in sorted(C.CASES) if n not in ("burgers3d_n16",)]
+SUPPORTED = sorted(C.CASES)
 
 
 def _run(name, device="cuda", dtype=torch.float32):
@@ -55,6 +55,16 @@ def test_deterministic():
     assert torch.equal(a, b)
 
 
-def test_3d_programs_are_reported_unsupported():
+def test_python_callable_source_is_reported_unsupported():
+    M = C.namespace("torchfsm_gb300")
+    op = M.operator.Laplacian() + M.operator.ImplicitSource(lambda u: u ** 2)
+    u0 = torch.rand(1, 1, 64, device="cuda")
     with pytest.raises(_lib.UnsupportedProgram):
-        _run("burgers3d_n16")
+        op.integrate(u_0=u0, mesh=[(0, 1, 64)], dt=0.01, step=2)
+
+
+def test_3d_axis_above_256_is_reported_unsupported():
+    M = C.namespace("torchfsm_gb300")
+    u0 = torch.rand(1, 3, 16, 16, 512, device="cuda")
+    with pytest.raises(_lib.UnsupportedProgram):
+        M.pde.Burgers(0.01).integrate(u_0=u0, mesh=[(0, 1, 16), (0, 1, 16), (0, 1, 512)], dt=0.01, step=1)

@@ -20,16 +20,21 @@ def test_oracle_matches_reference(name):
     case = C.CASES[name]
     g = _load(name)
     u0 = C.initial_condition(name)
-    np.testing.assert_array_equal(u0, g["u0"])  # the seeded generator is reproducible
+    if "u0" in g:
+        np.testing.assert_array_equal(u0, g["u0"])  # the seeded generator is reproducible
+    # float64 fixtures pin the oracle to 1e-10; large fixtures are stored in float32
+    def tol(x):
+        return 1e-10 if x.dtype == np.float64 else 1e-6
+
     lin, nl = C.oracle_terms(name)
     final, traj = S.integrate(
         u0, case["mesh"], lin, nl, case["dt"], case["step"],
         integrator=case.get("integrator", "auto"), record=C.record_fn(name),
     )
-    assert S.rel_l2(final, g["final"]) < 1e-10
+    assert S.rel_l2(final, g["final"]) < tol(g["final"])
     if "traj" in g:
         assert traj.shape == g["traj"].shape
-        assert S.rel_l2(traj, g["traj"]) < 1e-10
+        assert S.rel_l2(traj, g["traj"]) < tol(g["traj"])
 
 
 @pytest.mark.parametrize("tag,dt_mesh", [

@@ -218,7 +218,7 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       break;
     case FSM_NL_CONVECTION:
       if (C != nd) return set_error(FSM_ERR_INVALID, "convection needs n_channel == ndim");
-      path = nd == 1 ? 1 : (nd == 2 ? 2 : 0);
+      path = nd == 1 ? 1 : (nd == 2 ? 2 : 4);
       break;
     case FSM_NL_VORTICITY:
       if (nd != 2 || C != 1) return set_error(FSM_ERR_INVALID, "vorticity convection needs a 2D scalar field");
@@ -226,16 +226,21 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       break;
     case FSM_NL_KS:
       if (C != 1) return set_error(FSM_ERR_INVALID, "KS convection needs a scalar field");
-      path = nd == 1 ? 1 : (nd == 2 ? 2 : 0);
+      path = nd == 1 ? 1 : (nd == 2 ? 2 : 4);
       break;
     case FSM_NL_LERAY:
       if (C != nd) return set_error(FSM_ERR_INVALID, "Leray-projected convection needs n_channel == ndim");
-      path = nd == 2 ? 2 : 0;
+      path = nd == 2 ? 2 : (nd == 3 ? 4 : 0);
       break;
     default:
       return set_error(FSM_ERR_INVALID, "unknown nonlinear term");
   }
   if (path == 0) return set_error(FSM_ERR_UNSUPPORTED, "no fused kernel for this program on a " + std::to_string(nd) + "D mesh");
+  if (path == 4) {
+    for (int i = 0; i < 3; ++i)
+      if (mesh->n[i] > 256)
+        return set_error(FSM_ERR_UNSUPPORTED, "3D fused kernels take 16..256 points per axis");
+  }
   if (integ == FSM_ETDRK0 && (nl != FSM_NL_NONE || prog->source))
     return set_error(FSM_ERR_INVALID, "ETDRK0 only supports linear programs");
   if (nl == FSM_NL_NONE && integ != FSM_ETDRK0 && !prog->source && scheme_stages(integ) == 0)
@@ -271,6 +276,10 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
   if (path == 2) {
     p->n_mid = (nl == FSM_NL_KS) ? 2 : 4;
     p->n_prod = (nl == FSM_NL_CONVECTION || nl == FSM_NL_LERAY) ? 2 : 1;
+  } else if (path == 4) {
+    p->n_mid = (nl == FSM_NL_KS) ? 2 : 2 * C;
+    p->n_mid2 = 3 * (p->n_mid / 2);
+    p->n_prod = (nl == FSM_NL_KS) ? 1 : C;
   }
 
   int rc = FSM_OK;
@@ -349,8 +358,8 @@ static size_t workspace_layout(const FsmPlan* p, int32_t batch, int32_t steps, s
   size_t bytes = align256((size_t)(steps + 1) * sizeof(int32_t));  // record slots
   bytes += 256;                                                    // KS batch-mean scratch
   if (off_arrays) *off_arrays = bytes;
-  if (p->path == 2) {
-    const size_t per = (size_t)(p->n_aux * p->C + p->n_mid + p->n_prod) * p->S * sizeof(float2);
+  if (p->path == 2 || p->path == 4) {
+    const size_t per = (size_t)(p->n_aux * p->C + p->n_mid + p->n_mid2 + p->n_prod) * p->S * sizeof(float2);
     bytes += align256(per * (size_t)batch);
   }
   return bytes;
@@ -364,8 +373,9 @@ int fsm_plan_workspace_bytes(const FsmPlan* plan, int32_t batch, int32_t steps, 
 
 int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches) {
   if (!plan || !launches || steps < 0) return set_error(FSM_ERR_INVALID, "launch_count arguments");
-  if (plan->path == 2) {
-    const int64_t per_stage = 2 + ((plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) ? 1 : 0);
+  if (plan->path == 2 || plan->path == 4) {
+    const int64_t per_stage = (plan->path == 4 ? 4 : 2) +
+                              ((plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) ? 1 : 0);
     *launches = 1 + (int64_t)steps * plan->nstages * per_stage;
   } else {
     *launches = 1;
@@ -444,6 +454,8 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   if (p->lin_batch > 1 && p->lin_batch != batch) return set_error(FSM_ERR_INVALID, "batch != lin_batch");
   if (p->source && p->src_batch > 1 && p->src_batch != batch) return set_error(FSM_ERR_INVALID, "batch != src_batch");
   if ((int64_t)batch * p->C > 65535 && p->path == 2) return set_error(FSM_ERR_UNSUPPORTED, "batch too large for one launch");
+  if (p->path == 4 && (int64_t)batch * p->n_prod * p->n[0] > 65535)
+    return set_error(FSM_ERR_UNSUPPORTED, "batch too large for one launch");
   bool any_record = false;
   if (record_slot) {
     for (int i = 0; i <= steps; ++i) {
@@ -478,8 +490,11 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.src_batch = p->src_batch;
   a.kx = p->kvec + p->koff[0];
   a.ky = p->kvec + p->koff[p->ndim - 1];
+  a.km = p->kvec + p->koff[p->ndim == 3 ? 1 : 0];
   a.keepx = p->keep + p->koff[0];
   a.keepy = p->keep + p->koff[p->ndim - 1];
+  a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
+  a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
   a.dc = (float2*)(ws + off_arrays - 256);
   a.coef = p->nl_coef;
@@ -488,6 +503,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.n_aux = p->n_aux;
   a.n_mid = p->n_mid;
   a.n_prod = p->n_prod;
+  a.n_mid2 = p->n_mid2;
   a.integ = p->integ;
   a.nstages = p->nstages;
   a.steps = steps;
@@ -499,21 +515,29 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   if (p->path == 3) return timed(prof, kProfOther, [&] { return launch_pointwise(p, a, st); });
   if (p->path == 1) return timed(prof, kProfOther, [&] { return launch_line(p, a, st); });
 
-  // plane passes
+  // plane (2D) / volume (3D) passes
   float2* arr = (float2*)(ws + off_arrays);
   const int64_t per_field = p->S;
   a.aux = arr;
   a.mid = a.aux + (int64_t)batch * p->n_aux * p->C * per_field;
-  a.prod = a.mid + (int64_t)batch * p->n_mid * per_field;
+  a.mid2 = a.mid + (int64_t)batch * p->n_mid * per_field;
+  a.prod = a.mid2 + (int64_t)batch * p->n_mid2 * per_field;
   a.slots = nullptr;
   const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
+  const bool vol = p->path == 4;
   a.stage = -1;
   a.emit = steps > 0;
   a.slot = record_slot ? record_slot[0] : -1;
   if ((rc = timed(prof, kProfPrime, [&] { return launch_plane_col(p, a, st); }))) return rc;
   for (int step = 0; step < steps; ++step) {
     for (int s = 0; s < p->nstages; ++s) {
-      if ((rc = timed(prof, kProfRow, [&] { return launch_plane_row(p, a, st); }))) return rc;
+      if (vol) {
+        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_inv(p, a, st); }))) return rc;
+        if ((rc = timed(prof, kProfRow, [&] { return launch_volume_axis2(p, a, st); }))) return rc;
+        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_fwd(p, a, st); }))) return rc;
+      } else {
+        if ((rc = timed(prof, kProfRow, [&] { return launch_plane_row(p, a, st); }))) return rc;
+      }
       if (ks_mean && (rc = timed(prof, kProfOther, [&] { return launch_ks_mean(p, a, st); }))) return rc;
       const bool last = s == p->nstages - 1;
       a.stage = s;
@@ -571,7 +595,9 @@ int fsm_rfftn(const FsmPlan* p, int32_t count, const float* in, void* out, void*
     int64_t outer = count;
     for (int j = 0; j < ax; ++j) outer *= p->n[j];
     if (outer > 65535) return set_error(FSM_ERR_UNSUPPORTED, "rfftn: too many fields in one call");
-    if ((rc = transform_c2c_strided(p->n[ax], false, (float2*)out, outer, inner, p->tw, st))) return rc;
+    rc = transform_c2c_strided_reg(p->n[ax], false, (float2*)out, outer, inner, p->tw, st);
+    if (rc == -1) rc = transform_c2c_strided(p->n[ax], false, (float2*)out, outer, inner, p->tw, st);
+    if (rc) return rc;
     inner *= p->n[ax];
   }
   return FSM_OK;
@@ -588,7 +614,9 @@ int fsm_irfftn(const FsmPlan* p, int32_t count, void* in, float* out, void* stre
     int64_t outer = count;
     for (int j = 0; j < ax; ++j) outer *= p->n[j];
     if (outer > 65535) return set_error(FSM_ERR_UNSUPPORTED, "irfftn: too many fields in one call");
-    if ((rc = transform_c2c_strided(p->n[ax], true, (float2*)in, outer, inner, p->tw, st))) return rc;
+    rc = transform_c2c_strided_reg(p->n[ax], true, (float2*)in, outer, inner, p->tw, st);
+    if (rc == -1) rc = transform_c2c_strided(p->n[ax], true, (float2*)in, outer, inner, p->tw, st);
+    if (rc) return rc;
     inner *= p->n[ax];
   }
   const int nl = p->n[nd - 1];

@@ -172,8 +172,8 @@ struct FsmPlan {
   int64_t tstride = 0;       // lin_batch * lin_ch * S
   float2* source = nullptr;  // [src_batch][C][S] or null
   // fused-path array counts per sample (2D / 3D)
-  int n_mid = 0, n_prod = 0, n_aux = 0;
-  int path = 0;  // 1: line kernel (1D), 2: plane passes (2D), 3: pointwise (no transform needed)
+  int n_mid = 0, n_prod = 0, n_aux = 0, n_mid2 = 0;
+  int path = 0;  // 1: line kernel (1D), 2: plane passes (2D), 3: pointwise, 4: volume passes (3D)
 };
 
 namespace fsm {

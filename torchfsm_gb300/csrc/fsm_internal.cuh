@@ -22,8 +22,13 @@ struct StepArgs {
   int src_batch;
   const float* kx;            // 2 pi f of the first axis
   const float* ky;            // 2 pi f of the last axis
+  const float* km;            // 2 pi f of the middle axis (3D)
   const uint8_t* keepx;
   const uint8_t* keepy;
+  const uint8_t* keepm;       // middle axis (3D)
+  float2* mid2;               // [B][n_mid2][S] fields after the middle-axis inverse transform (3D)
+  int n_mid2;
+  int nm;                     // points of the middle axis (3D)
   const float2* tw;           // master twiddles
   float2* dc;                 // batch-mean scratch of the KS mean removal
   float coef;                 // nonlinear coefficient
@@ -50,6 +55,12 @@ int launch_nonfinite(const float2* f, int64_t count, int64_t S, int32_t* flags, 
 int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
                              size_t workspace_bytes, cudaStream_t st);
 size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps);
+
+int transform_c2c_strided_reg(int n, bool inverse, float2* data, int64_t outer, int64_t inner, const float2* tw,
+                              cudaStream_t st);  // -1: no register kernel for n
+int launch_volume_axis1_inv(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_volume_axis2(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+int launch_volume_axis1_fwd(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 // Register-FFT plane passes (64..256 points per axis); return -1 when no kernel covers the sizes.

@@ -20,10 +20,14 @@
 
 namespace fsm {
 
-template <int KIND>
+template <int KIND, int DIM>
 struct RegKind {
-  static constexpr int C = (KIND == FSM_NL_CONVECTION || KIND == FSM_NL_LERAY) ? 2 : 1;
-  static constexpr int NM = (KIND == FSM_NL_KS) ? 2 : 4;
+  // channels of the state
+  static constexpr int C = (KIND == FSM_NL_CONVECTION || KIND == FSM_NL_LERAY) ? DIM : 1;
+  // channels whose stage update runs together (the Leray projection mixes all of them)
+  static constexpr int CG = (KIND == FSM_NL_LERAY) ? C : 1;
+  // mid fields written per channel group
+  static constexpr int NMG = (KIND == FSM_NL_VORTICITY) ? 4 : 2 * CG;
 };
 
 template <int NX>
@@ -36,132 +40,173 @@ struct ColCfg {
   static constexpr int P = NEED | 1;  // odd pitch: a row across W columns hits W distinct banks
 };
 
-template <int NX, int KIND>
-__global__ void __launch_bounds__(256) k_plane_col_r(StepArgs a) {
+// Wavenumbers and dealias factor of the point (row, inner index j). 2D: j is
+// the last-axis index; 3D: j = jm * H + jl (middle, last axis).
+template <int DIM>
+struct PointK {
+  float kx, ky, kz;  // ky: second axis, kz: third axis (3D)
+  float mask;
+};
+
+template <int DIM>
+__device__ __forceinline__ PointK<DIM> point_k(const StepArgs& a, int row, int64_t j) {
+  PointK<DIM> p;
+  p.kx = a.kx[row];
+  if (DIM == 2) {
+    p.ky = a.ky[j];
+    p.kz = 0.f;
+    p.mask = (float)(a.keepx[row] & a.keepy[j]);
+  } else {
+    const int jm = (int)(j / a.H), jl = (int)(j % a.H);
+    p.ky = a.km[jm];
+    p.kz = a.ky[jl];
+    p.mask = (float)(a.keepx[row] & a.keepm[jm] & a.keepy[jl]);
+  }
+  p.mask *= a.scale;
+  return p;
+}
+
+// Axis-0 pass (2D: the column pass; 3D: the x pass). A CTA owns W adjacent
+// inner columns (contiguous in memory) of one sample, all NX rows:
+//   1. forward transform along axis 0 of the products -> N (+ Leray projection, + source)
+//   2. stage update at every point, recording when a step completes
+//   3. next stage field (mask, 1/N, i kx, streamfunction) -> inverse transform -> mid fields
+// Channels are processed in groups so that Convection needs one staging tile.
+template <int NX, int KIND, int DIM>
+__global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
   using Cfg = ColCfg<NX>;
-  using K = RegKind<KIND>;
-  constexpr int T = Cfg::T, E = Cfg::E, W = Cfg::W, P = Cfg::P, C = K::C;
+  using K = RegKind<KIND, DIM>;
+  constexpr int T = Cfg::T, E = Cfg::E, W = Cfg::W, P = Cfg::P, C = K::C, CG = K::CG;
   extern __shared__ float2 smem[];
-  float2* twt = smem;                   // NX
-  float2* tileA = smem + NX;            // C * W * P: products -> N -> next stage field
-  float2* tileB = tileA + C * W * P;    // W * P: transpose scratch and output staging
+  float2* twt = smem;                 // NX
+  float2* tileA = smem + NX;          // CG * W * P: products -> N -> next stage field
+  float2* tileB = tileA + CG * W * P; // W * P: transpose scratch and output staging
   const int g = threadIdx.x / T, t = threadIdx.x % T;
   const int b = blockIdx.y;
-  const int c0 = blockIdx.x * W;
-  const int H = a.H;
+  const int64_t c0 = (int64_t)blockIdx.x * W;
   const int64_t S = a.S;
+  const int64_t inner = S / NX;
   load_reg_twiddles<NX>(twt, a.tw, threadIdx.x, 256);
-
-  if (a.stage >= 0) {
-    for (int f = 0; f < C; ++f) {
-      const float2* src = a.prod + ((int64_t)b * a.n_prod + f) * S;
-      for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
-        const int row = idx / W, col = idx % W;
-        if (c0 + col < H) tileA[(f * W + col) * P + row] = src[(int64_t)row * H + c0 + col];
-      }
-    }
-    __syncthreads();
-    for (int f = 0; f < C; ++f) {
-      float2* colp = tileA + (f * W + g) * P;
-      float2 v[E];
-#pragma unroll
-      for (int j = 0; j < E; ++j) v[j] = colp[t + T * j];
-      reg_fft<NX, false>(v, tileB + g * P, twt, t);
-#pragma unroll
-      for (int j = 0; j < E; ++j) colp[t + T * j] = v[j];
-    }
-  }
-  __syncthreads();
-
   const bool last = a.stage == a.nstages - 1;
-  for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
-    const int row = idx / W, col = idx % W;
-    const int ky_i = c0 + col;
-    if (ky_i >= H) continue;
-    const int64_t sidx = (int64_t)row * H + ky_i;
-    float2 nv[C];
-    if (a.stage >= 0) {
-#pragma unroll
-      for (int c = 0; c < C; ++c) nv[c] = tileA[(c * W + col) * P + row];
-      if (KIND == FSM_NL_LERAY) {
-        const float kxv = a.kx[row], kyv = a.ky[ky_i];
-        const float lap = -(kxv * kxv + kyv * kyv);
-        const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-        const float2 div = cadd(cscale(cmuli(nv[0]), kxv), cscale(cmuli(nv[1]), kyv));
-        const float2 pr = cscale(div, il);
-        const float2 n0 = csub(cscale(cmuli(pr), kxv), nv[0]);
-        const float2 n1 = csub(cscale(cmuli(pr), kyv), nv[1]);
-        nv[0] = n0;
-        nv[1] = n1;
-      }
-      if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && ky_i == 0) nv[0] = csub(nv[0], a.dc[0]);
-#pragma unroll
-      for (int c = 0; c < C; ++c) {
-        nv[c] = cscale(nv[c], a.coef);
-        if (a.src) nv[c] = cadd(nv[c], a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
-      }
-    }
-    const float m = (float)(a.keepx[row] & a.keepy[ky_i]) * a.scale;
-#pragma unroll
-    for (int c = 0; c < C; ++c) {
-      float2* up = a.state + ((int64_t)b * C + c) * S + sidx;
-      float2 st;
-      if (a.stage < 0) {
-        st = *up;
-      } else {
-        float2* accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
-        float2* qp = a.aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
-        const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
-        st = etd_stage(a.integ, a.stage, nv[c], up, accp, qp, a.tab + toff, a.ts);
-      }
-      if (a.slot >= 0 && (a.stage < 0 || last)) a.traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
-      tileA[(c * W + col) * P + row] = cscale(st, m);
-    }
-  }
-  if (!a.emit) return;
-  __syncthreads();
-
-  const int col = c0 + g;
-  const float kyv = a.ky[col < H ? col : H - 1];
   float kxr[E];
 #pragma unroll
   for (int j = 0; j < E; ++j) kxr[j] = a.kx[t + T * j];
-  for (int mf = 0; mf < K::NM; ++mf) {
-    const int c = (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) ? 0 : (mf >> 1);
-    const float2* colp = tileA + (c * W + g) * P;
-    float2 v[E];
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const float2 d = colp[t + T * j];
-      const float kxv = kxr[j];
-      float2 x;
-      if (KIND == FSM_NL_VORTICITY) {
-        // 0: psi = -w/lap, 1: i kx psi, 2: w, 3: i kx w
-        if (mf < 2) {
-          const float lap = -(kxv * kxv + kyv * kyv);
-          const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-          const float2 psi = cscale(d, -il);
-          x = (mf == 0) ? psi : cscale(cmuli(psi), kxv);
-        } else {
-          x = (mf == 2) ? d : cscale(cmuli(d), kxv);
+  const int64_t gcol = c0 + g;
+  const PointK<DIM> gk = point_k<DIM>(a, 0, gcol < inner ? gcol : inner - 1);
+
+  for (int cg = 0; cg < C / CG; ++cg) {
+    if (a.stage >= 0) {
+      for (int f = 0; f < CG; ++f) {
+        const float2* src = a.prod + ((int64_t)b * a.n_prod + cg * CG + f) * S;
+        for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+          const int row = idx / W, col = idx % W;
+          if (c0 + col < inner) tileA[(f * W + col) * P + row] = src[(int64_t)row * inner + c0 + col];
         }
-      } else {
-        // KS: 0: phi, 1: i kx phi; convection: 2c: u_c, 2c+1: i kx u_c
-        x = (mf & 1) ? cscale(cmuli(d), kxv) : d;
       }
-      v[j] = x;
-    }
-    float2* ob = tileB + g * P;
-    reg_fft<NX, true>(v, ob, twt, t);
+      __syncthreads();
+      for (int f = 0; f < CG; ++f) {
+        float2* colp = tileA + (f * W + g) * P;
+        float2 v[E];
 #pragma unroll
-    for (int j = 0; j < E; ++j) ob[t + T * j] = v[j];
-    __syncthreads();
-    float2* dst = a.mid + ((int64_t)b * a.n_mid + mf) * S;
-    for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
-      const int row = idx / W, cc = idx % W;
-      if (c0 + cc < H) dst[(int64_t)row * H + c0 + cc] = tileB[cc * P + row];
+        for (int j = 0; j < E; ++j) v[j] = colp[t + T * j];
+        reg_fft<NX, false>(v, tileB + g * P, twt, t);
+#pragma unroll
+        for (int j = 0; j < E; ++j) colp[t + T * j] = v[j];
+      }
     }
     __syncthreads();
+
+    for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+      const int row = idx / W, col = idx % W;
+      const int64_t j = c0 + col;
+      if (j >= inner) continue;
+      const int64_t sidx = (int64_t)row * inner + j;
+      const PointK<DIM> pk = point_k<DIM>(a, row, j);
+      float2 nv[CG];
+      if (a.stage >= 0) {
+#pragma unroll
+        for (int f = 0; f < CG; ++f) nv[f] = tileA[(f * W + col) * P + row];
+        if (KIND == FSM_NL_LERAY) {
+          // conv -> i k p - conv with p = (i k . conv) / lap (1 where lap == 0)
+          const float kk[3] = {pk.kx, pk.ky, pk.kz};
+          float lap = 0.f;
+          float2 div = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int f = 0; f < CG; ++f) {
+            lap -= kk[f] * kk[f];
+            div = cadd(div, cscale(cmuli(nv[f]), kk[f]));
+          }
+          const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+          const float2 pr = cscale(div, il);
+#pragma unroll
+          for (int f = 0; f < CG; ++f) nv[f] = csub(cscale(cmuli(pr), kk[f]), nv[f]);
+        }
+        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv[0] = csub(nv[0], a.dc[0]);
+#pragma unroll
+        for (int f = 0; f < CG; ++f) {
+          const int c = cg * CG + f;
+          nv[f] = cscale(nv[f], a.coef);
+          if (a.src) nv[f] = cadd(nv[f], a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
+        }
+      }
+#pragma unroll
+      for (int f = 0; f < CG; ++f) {
+        const int c = cg * CG + f;
+        float2* up = a.state + ((int64_t)b * C + c) * S + sidx;
+        float2 st;
+        if (a.stage < 0) {
+          st = *up;
+        } else {
+          float2* accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
+          float2* qp = a.aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
+          const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+          st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, a.tab + toff, a.ts);
+        }
+        if (a.slot >= 0 && (a.stage < 0 || last)) a.traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
+        tileA[(f * W + col) * P + row] = cscale(st, pk.mask);
+      }
+    }
+    if (!a.emit) continue;  // uniform: no further barriers in this group
+    __syncthreads();
+
+    for (int mf = 0; mf < K::NMG; ++mf) {
+      const int f = (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) ? 0 : (mf >> 1);
+      const float2* colp = tileA + (f * W + g) * P;
+      float2 v[E];
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        const float2 d = colp[t + T * j];
+        const float kxv = kxr[j];
+        float2 x;
+        if (KIND == FSM_NL_VORTICITY) {
+          // 0: psi = -w/lap, 1: i kx psi, 2: w, 3: i kx w
+          if (mf < 2) {
+            const float lap = -(kxv * kxv + gk.ky * gk.ky);
+            const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+            const float2 psi = cscale(d, -il);
+            x = (mf == 0) ? psi : cscale(cmuli(psi), kxv);
+          } else {
+            x = (mf == 2) ? d : cscale(cmuli(d), kxv);
+          }
+        } else {
+          // KS: 0: phi, 1: i kx phi; convection (per channel): u_c, i kx u_c
+          x = (mf & 1) ? cscale(cmuli(d), kxv) : d;
+        }
+        v[j] = x;
+      }
+      float2* ob = tileB + g * P;
+      reg_fft<NX, true>(v, ob, twt, t);
+#pragma unroll
+      for (int j = 0; j < E; ++j) ob[t + T * j] = v[j];
+      __syncthreads();
+      const int mout = (KIND == FSM_NL_CONVECTION) ? cg * 2 + mf : mf;
+      float2* dst = a.mid + ((int64_t)b * a.n_mid + mout) * S;
+      for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+        const int row = idx / W, cc = idx % W;
+        if (c0 + cc < inner) dst[(int64_t)row * inner + c0 + cc] = tileB[cc * P + row];
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -313,16 +358,17 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
   }
 }
 
-template <int NX, int KIND>
-static int launch_col_r(const StepArgs& a, cudaStream_t st) {
+template <int NX, int KIND, int DIM>
+static int launch_axis0_r(const StepArgs& a, cudaStream_t st) {
   using Cfg = ColCfg<NX>;
-  using K = RegKind<KIND>;
-  const size_t smem = (size_t)(NX + (K::C + 1) * Cfg::W * Cfg::P) * sizeof(float2);
-  int rc = prep_smem(k_plane_col_r<NX, KIND>, smem);
+  using K = RegKind<KIND, DIM>;
+  const size_t smem = (size_t)(NX + (K::CG + 1) * Cfg::W * Cfg::P) * sizeof(float2);
+  int rc = prep_smem(k_axis0_r<NX, KIND, DIM>, smem);
   if (rc) return rc;
-  dim3 grid((a.H + Cfg::W - 1) / Cfg::W, a.B);
-  k_plane_col_r<NX, KIND><<<grid, 256, smem, st>>>(a);
-  return cuda_check(cudaGetLastError(), "k_plane_col_r");
+  const int64_t inner = a.S / NX;
+  dim3 grid((unsigned)((inner + Cfg::W - 1) / Cfg::W), a.B);
+  k_axis0_r<NX, KIND, DIM><<<grid, 256, smem, st>>>(a);
+  return cuda_check(cudaGetLastError(), "k_axis0_r");
 }
 
 template <int NY, int KIND>
@@ -340,12 +386,14 @@ static int launch_row_r(int nx, const StepArgs& a, cudaStream_t st) {
   return cuda_check(cudaGetLastError(), "k_plane_row_r");
 }
 
-template <int KIND>
+template <int KIND, int DIM>
 static int col_r_dispatch(int nx, const StepArgs& a, cudaStream_t st) {
   switch (nx) {
-    case 64: return launch_col_r<64, KIND>(a, st);
-    case 128: return launch_col_r<128, KIND>(a, st);
-    case 256: return launch_col_r<256, KIND>(a, st);
+    case 16: return launch_axis0_r<16, KIND, DIM>(a, st);
+    case 32: return launch_axis0_r<32, KIND, DIM>(a, st);
+    case 64: return launch_axis0_r<64, KIND, DIM>(a, st);
+    case 128: return launch_axis0_r<128, KIND, DIM>(a, st);
+    case 256: return launch_axis0_r<256, KIND, DIM>(a, st);
   }
   return -1;
 }
@@ -354,6 +402,8 @@ template <int KIND>
 static int row_r_dispatch(int nx, int ny, const StepArgs& a, cudaStream_t st) {
   if (nx < 2) return -1;
   switch (ny) {
+    case 16: return launch_row_r<16, KIND>(nx, a, st);
+    case 32: return launch_row_r<32, KIND>(nx, a, st);
     case 64: return launch_row_r<64, KIND>(nx, a, st);
     case 128: return launch_row_r<128, KIND>(nx, a, st);
     case 256: return launch_row_r<256, KIND>(nx, a, st);
@@ -363,11 +413,19 @@ static int row_r_dispatch(int nx, int ny, const StepArgs& a, cudaStream_t st) {
 
 // Returns -1 when no register-FFT kernel exists for the sizes (caller falls back).
 int launch_plane_col_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
+  if (p->ndim == 3) {
+    switch (p->nl) {
+      case FSM_NL_CONVECTION: return col_r_dispatch<FSM_NL_CONVECTION, 3>(p->n[0], a, st);
+      case FSM_NL_LERAY: return col_r_dispatch<FSM_NL_LERAY, 3>(p->n[0], a, st);
+      case FSM_NL_KS: return col_r_dispatch<FSM_NL_KS, 3>(p->n[0], a, st);
+    }
+    return -1;
+  }
   switch (p->nl) {
-    case FSM_NL_VORTICITY: return col_r_dispatch<FSM_NL_VORTICITY>(p->n[0], a, st);
-    case FSM_NL_CONVECTION: return col_r_dispatch<FSM_NL_CONVECTION>(p->n[0], a, st);
-    case FSM_NL_LERAY: return col_r_dispatch<FSM_NL_LERAY>(p->n[0], a, st);
-    case FSM_NL_KS: return col_r_dispatch<FSM_NL_KS>(p->n[0], a, st);
+    case FSM_NL_VORTICITY: return col_r_dispatch<FSM_NL_VORTICITY, 2>(p->n[0], a, st);
+    case FSM_NL_CONVECTION: return col_r_dispatch<FSM_NL_CONVECTION, 2>(p->n[0], a, st);
+    case FSM_NL_LERAY: return col_r_dispatch<FSM_NL_LERAY, 2>(p->n[0], a, st);
+    case FSM_NL_KS: return col_r_dispatch<FSM_NL_KS, 2>(p->n[0], a, st);
   }
   return -1;
 }

@@ -79,13 +79,17 @@ __global__ void __launch_bounds__(256) k_plane_col(StepArgs a) {
 #pragma unroll
       for (int c = 0; c < C; ++c) nv[c] = fld[(c * kTileW + col) * P + row];
       if (KIND == FSM_NL_LERAY) {
-        // conv -> i k p - conv with p = (i kx conv0 + i ky conv1) / lap (1 where lap == 0)
+        // conv -> i k p - conv with p = (i kx conv0 + i ky conv1) / lap (1 where lap == 0); at the
+        // x Nyquist row with ky strictly inside, the Hermitian part keeps the two axes apart
+        // (see nv_leray in fsm_plane_reg.cu)
         const float lap = -(kxv * kxv + kyv * kyv);
         const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-        const float2 div = cadd(cscale(cmuli(nv[0]), kxv), cscale(cmuli(nv[1]), kyv));
-        const float2 pr = cscale(div, il);
-        const float2 n0 = csub(cscale(cmuli(pr), kxv), nv[0]);
-        const float2 n1 = csub(cscale(cmuli(pr), kyv), nv[1]);
+        const float2 dx = cscale(cmuli(nv[0]), kxv), dy = cscale(cmuli(nv[1]), kyv);
+        const bool split = (row == NX / 2) && ky_i > 0 && ky_i < H - 1;
+        const float2 p0 = cscale(split ? dx : cadd(dx, dy), il);
+        const float2 p1 = cscale(split ? dy : cadd(dx, dy), il);
+        const float2 n0 = csub(cscale(cmuli(p0), kxv), nv[0]);
+        const float2 n1 = csub(cscale(cmuli(p1), kyv), nv[1]);
         nv[0] = n0;
         nv[1] = n1;
       }

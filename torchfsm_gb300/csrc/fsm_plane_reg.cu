@@ -66,6 +66,48 @@ __device__ __forceinline__ PointK<DIM> point_k(const StepArgs& a, int row, int64
   return p;
 }
 
+// Leray projection of the convection term at one point: N_c = i k_c p - conv_c,
+// p = (sum_i i k_i conv_i) / lap (1 where lap == 0), operator/dedicated/_navier_stokes.py:246-254.
+// The state stores only the last axis' first half, so at points whose mirror -k
+// is not stored (last-axis index strictly inside) the kernel must advance the
+// Hermitian part (N(k) + conj N(-k)) / 2, which is what ifftn(...).real of the
+// reference's state follows. Where a non-last axis sits at its Nyquist index its
+// wavenumber does not change sign under k -> -k, and that Hermitian part is the
+// projection restricted to axes with the same Nyquist status as c.
+template <int DIM, int CG>
+__device__ __forceinline__ void nv_leray(float2 (&nv)[CG], const PointK<DIM>& pk, int row, int64_t j,
+                                         const StepArgs& a, int nx) {
+  const float kk[3] = {pk.kx, pk.ky, pk.kz};
+  float sgn[3] = {1.f, 1.f, 1.f};
+  int jl, jm = 0;
+  if (DIM == 2) {
+    jl = (int)j;
+  } else {
+    jm = (int)(j / a.H);
+    jl = (int)(j % a.H);
+  }
+  const bool inside = jl > 0 && jl < a.H - 1;
+  if (inside) {
+    if (row == nx / 2) sgn[0] = -1.f;
+    if (DIM == 3 && jm == a.nm / 2) sgn[1] = -1.f;
+  }
+  float lap = 0.f;
+#pragma unroll
+  for (int f = 0; f < CG; ++f) lap -= kk[f] * kk[f];
+  const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+  float2 out[CG];
+#pragma unroll
+  for (int c = 0; c < CG; ++c) {
+    float2 div = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int f = 0; f < CG; ++f)
+      if (sgn[f] == sgn[c]) div = cadd(div, cscale(cmuli(nv[f]), kk[f]));
+    out[c] = csub(cscale(cmuli(cscale(div, il)), kk[c]), nv[c]);
+  }
+#pragma unroll
+  for (int c = 0; c < CG; ++c) nv[c] = out[c];
+}
+
 // Axis-0 pass (2D: the column pass; 3D: the x pass). A CTA owns W adjacent
 // inner columns (contiguous in memory) of one sample, all NX rows:
 //   1. forward transform along axis 0 of the products -> N (+ Leray projection, + source)
@@ -116,54 +158,51 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
     }
     __syncthreads();
 
-    for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
-      const int row = idx / W, col = idx % W;
-      const int64_t j = c0 + col;
-      if (j >= inner) continue;
-      const int64_t sidx = (int64_t)row * inner + j;
-      const PointK<DIM> pk = point_k<DIM>(a, row, j);
-      float2 nv[CG];
-      if (a.stage >= 0) {
+    {
+      // restrict-qualified views so that loads of later points may be issued ahead of the stores of earlier ones
+      float2* __restrict__ state = a.state;
+      float2* __restrict__ aux = a.aux;
+      float2* __restrict__ traj = a.traj;
+      const float2* __restrict__ tab = a.tab;
+      const float2* __restrict__ srcp = a.src;
+      constexpr int PPT = NX * W / 256;  // points per thread
+#pragma unroll 4
+      for (int it = 0; it < PPT; ++it) {
+        const int idx = threadIdx.x + it * 256;
+        const int row = idx / W, col = idx % W;
+        const int64_t j = c0 + col;
+        if (j >= inner) continue;
+        const int64_t sidx = (int64_t)row * inner + j;
+        const PointK<DIM> pk = point_k<DIM>(a, row, j);
+        float2 nv[CG];
+        if (a.stage >= 0) {
 #pragma unroll
-        for (int f = 0; f < CG; ++f) nv[f] = tileA[(f * W + col) * P + row];
-        if (KIND == FSM_NL_LERAY) {
-          // conv -> i k p - conv with p = (i k . conv) / lap (1 where lap == 0)
-          const float kk[3] = {pk.kx, pk.ky, pk.kz};
-          float lap = 0.f;
-          float2 div = make_float2(0.f, 0.f);
+          for (int f = 0; f < CG; ++f) nv[f] = tileA[(f * W + col) * P + row];
+          if (KIND == FSM_NL_LERAY) nv_leray<DIM, CG>(nv, pk, row, j, a, NX);
+          if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv[0] = csub(nv[0], a.dc[0]);
 #pragma unroll
           for (int f = 0; f < CG; ++f) {
-            lap -= kk[f] * kk[f];
-            div = cadd(div, cscale(cmuli(nv[f]), kk[f]));
+            const int c = cg * CG + f;
+            nv[f] = cscale(nv[f], a.coef);
+            if (srcp) nv[f] = cadd(nv[f], srcp[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
           }
-          const float il = (lap == 0.f) ? 1.f : 1.f / lap;
-          const float2 pr = cscale(div, il);
-#pragma unroll
-          for (int f = 0; f < CG; ++f) nv[f] = csub(cscale(cmuli(pr), kk[f]), nv[f]);
         }
-        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv[0] = csub(nv[0], a.dc[0]);
 #pragma unroll
         for (int f = 0; f < CG; ++f) {
           const int c = cg * CG + f;
-          nv[f] = cscale(nv[f], a.coef);
-          if (a.src) nv[f] = cadd(nv[f], a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
+          float2* up = state + ((int64_t)b * C + c) * S + sidx;
+          float2 st;
+          if (a.stage < 0) {
+            st = *up;
+          } else {
+            float2* accp = aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
+            float2* qp = aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
+            const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+            st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, tab + toff, a.ts);
+          }
+          if (a.slot >= 0 && (a.stage < 0 || last)) traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
+          tileA[(f * W + col) * P + row] = cscale(st, pk.mask);
         }
-      }
-#pragma unroll
-      for (int f = 0; f < CG; ++f) {
-        const int c = cg * CG + f;
-        float2* up = a.state + ((int64_t)b * C + c) * S + sidx;
-        float2 st;
-        if (a.stage < 0) {
-          st = *up;
-        } else {
-          float2* accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
-          float2* qp = a.aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
-          const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
-          st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, a.tab + toff, a.ts);
-        }
-        if (a.slot >= 0 && (a.stage < 0 || last)) a.traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
-        tileA[(f * W + col) * P + row] = cscale(st, pk.mask);
       }
     }
     if (!a.emit) continue;  // uniform: no further barriers in this group

@@ -77,14 +77,10 @@ def cpu_reference_throughput(samples: int, time_steps: int, threads: int) -> dic
         S.integrate(w0[i : i + 1], MESH, [(1.0 / RE, ("laplacian",))], [(-1.0, "vorticity_convection")], DT,
                     time_steps, real_dtype=np.float32)
 
-    # coefficient build outside the timed region, as for the GPU path
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
         list(ex.map(one, range(samples)))
-    t1 = time.perf_counter()
-    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-        list(ex.map(lambda i: None, range(samples)))
-    elapsed = t1 - t0
+    elapsed = time.perf_counter() - t0
     dof_steps = samples * N * N * time_steps
     return {"value": dof_steps / elapsed, "unit": "DOF*steps/s", "cores": threads, "kind": "port",
             "sample": f"{samples} samples x {time_steps} SETDRK4 steps of the 256^2 workload "
@@ -268,14 +264,223 @@ def row_pass_bytes(B: int) -> float:
     return 5.0 * 8.0 * B * N * H
 
 
-def ncu_case():
-    """Full batch (inputs larger than L2), 3 SETDRK4 steps: 25 launches after a 9-launch warm-up."""
+# ---------------------------------------------------------------------------
+# other workloads (one JSON line each; the default workload is the headline)
+# ---------------------------------------------------------------------------
+def _pctl(xs, q):
+    xs = sorted(xs)
+    return xs[min(len(xs) - 1, int(round(q / 100.0 * (len(xs) - 1))))]
+
+
+def run_burgers1d(args):
+    """1D viscous Burgers, N = 128, nu = 0.01, L = 1, u0 = sin(2 pi x) + 0.5, dt = 0.01, 200 steps,
+    batch 1, AutoRecorder (201 frames): solve latency through the public API."""
     import torch
 
     import __graft_entry__ as entry
 
     entry.build()
+    from oracle import spectral as S
     from torchfsm_gb300 import pde
+    from torchfsm_gb300.traj_recorder import AutoRecorder
+
+    n, steps, dt = 128, 200, 0.01
+    mesh = [(0.0, 1.0, n)]
+    x = np.arange(n) / n
+    u0h = torch.tensor((np.sin(2 * np.pi * x) + 0.5).reshape(1, 1, n), dtype=torch.float32).pin_memory()
+    op = pde.Burgers(0.01)
+    device = torch.device("cuda", 0)
+    op.integrate(u_0=u0h.to(device), mesh=mesh, dt=dt, step=1)
+    lat = []
+    for i in range(args.warmup + max(args.steps, 20)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rec = AutoRecorder()
+        traj = op.integrate(u_0=u0h.to(device, non_blocking=True), dt=dt, step=steps, trajectory_recorder=rec)
+        out = traj.cpu()
+        t1 = time.perf_counter()
+        if i >= args.warmup:
+            lat.append((t1 - t0) * 1e3)
+    # device time of the fused kernel alone (one launch for all 200 steps and the 201 frames)
+    integ = op._state_dict["integrator"]
+    state0 = integ.spectral.to_half(u0h.to(device))
+    traj_h = torch.empty((1, steps + 1, 1, n // 2 + 1), dtype=torch.complex64, device=device)
+    ws = torch.empty(integ.plan.workspace_bytes(1, steps), dtype=torch.uint8, device=device)
+    dev = []
+    for i in range(args.warmup + 20):
+        st = state0.clone()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        integ.plan.integrate_half(st, steps, slots=list(range(steps + 1)), traj=traj_h, workspace=ws)
+        e1.record()
+        e1.synchronize()
+        if i >= args.warmup:
+            dev.append(e0.elapsed_time(e1))
+    u0 = np.sin(2 * np.pi * x).reshape(1, 1, n) + 0.5
+    _, ref = S.integrate(u0, mesh, [(0.01, ("laplacian",))], [(-1.0, "convection")], dt, steps, record=lambda i: True)
+    err = S.rel_l2(out.numpy(), ref)
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        S.integrate(u0.astype(np.float32), mesh, [(0.01, ("laplacian",))], [(-1.0, "convection")], dt, steps,
+                    record=lambda i: True, real_dtype=np.float32)
+    cpu_s = (time.perf_counter() - t0) / reps
+    p50 = _pctl(lat, 50)
+    line = {"metric": "DOF*steps/s (1D Burgers N=128, 200 SETDRK4 steps, 201 recorded frames)",
+            "value": n * steps / (statistics.median(dev) * 1e-3), "unit": "DOF*steps/s", "n_gpus": 1,
+            "steps": len(lat), "warmup": args.warmup, "ms_per_step": statistics.median(dev),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/c64",
+            "data": "u0 = sin(2 pi x) + 0.5",
+            "config": {"workload": "burgers1d_n128_200steps", "rel_l2_traj_vs_fp64": err},
+            "latency_ms": {"p50": p50, "p99": _pctl(lat, 99), "n": len(lat),
+                           "what": "Burgers(0.01).integrate with AutoRecorder, pinned host u0 in, trajectory out"},
+            "e2e": {"value": n * steps / (p50 * 1e-3), "unit": "DOF*steps/s", "h2d_bytes_per_step": n * 4,
+                    "d2h_bytes_per_step": out.numel() * 4},
+            "gpu_launches": 1,
+            "roofline": {"bound": "latency", "note": "one 128-point line per CTA; all 200 steps in one launch",
+                         "device_ms": statistics.median(dev)},
+            "cpu_baseline": {"value": n * steps / cpu_s, "unit": "DOF*steps/s", "cores": 1, "kind": "port",
+                             "sample": "the whole workload, numpy complex64 restatement, 1 thread"}}
+    print(json.dumps(line))
+
+
+def run_burgers3d(args):
+    """3D viscous Burgers (3 channels), 256^3, nu = 0.005, dt = 1e-3, 200 steps, batch 1,
+    u0 = GRF with E(k) ~ k^2 exp(-(k/3)^2)."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    entry.build()
+    from torchfsm_gb300 import initial, pde
+
+    n, steps, dt = 256, 200, 1e-3
+    mesh = [(0.0, 2 * math.pi, n)] * 3
+    device = torch.device("cuda", 0)
+    u0 = torch.tensor(initial.gaussian_random_field((n, n, n), 1, 3, initial.velocity_spectrum, SEED)
+                      .astype(np.float32), device=device)
+    op = pde.Burgers(0.005)
+    op.integrate(u_0=u0, mesh=mesh, dt=dt, step=1)
+    integ = op._state_dict["integrator"]
+    plan = integ.plan
+    state0 = integ.spectral.to_half(u0)
+    state = state0.clone()
+    ws = torch.empty(plan.workspace_bytes(1, steps), dtype=torch.uint8, device=device)
+    for _ in range(args.warmup):
+        state.copy_(state0)
+        plan.integrate_half(state, steps, workspace=ws)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            state.copy_(state0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            plan.integrate_half(state, steps, workspace=ws)
+            e1.record()
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    dof_steps = 3 * n ** 3 * steps
+    prof = profile_kernels(plan, state0, ws, device)
+    finite = bool(torch.isfinite(torch.view_as_real(state)).all().item())
+    line = {"metric": "DOF*steps/s (3D Burgers 256^3 x 3 channels, SETDRK4, FP32)", "value": dof_steps / (ms * 1e-3),
+            "unit": "DOF*steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/c64",
+            "data": "synthetic (seeded GRF velocity)",
+            "config": {"workload": "burgers3d_256cubed_200steps", "result_finite": finite,
+                       "l2": "inputs (200 MB state, 1.6 GB workspace) larger than L2"},
+            "gpu_launches": plan.launch_count(steps) * args.steps,
+            "roofline": {"bound": "hbm", "per_kernel_ms": {k: v["avg_ms"] for k, v in prof.items() if v["launches"]},
+                         "step_model_bytes_per_dof_step": 276,
+                         "step_achieved_gbs": 276.0 * dof_steps / (ms * 1e-3) / 1e9, "peak": _peaks()[0]},
+            "clocks": clk.summary()}
+    print(json.dumps(line))
+
+
+def run_serving(args):
+    """Mixed request stream (KS 1D N=256..4096 / 2D Burgers N=64..256, batch 1-32, steps 100-2000,
+    dt 0.01-0.1): the continuous-batching server against the plain drop-in run one solve at a time."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    entry.build()
+    from torchfsm_gb300 import serving
+
+    device = torch.device("cuda", 0)
+    count = args.requests
+    reqs = serving.make_stream(count, seed=7, rate_hz=0.0)
+    server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk)
+    server.prepare(sorted({(r.kind, r.n) for r in reqs}))
+    # warm-up: a few requests through both paths (kernel attributes, plans of the plain path)
+    warm = serving.make_stream(8, seed=99, rate_hz=0.0, max_steps=120)
+    server.run(warm, realtime=False)
+    ops = {}
+    for r in warm:
+        serving.solve_alone(r, device, ops)
+    total = sum(r.dof_steps for r in reqs)
+    # burst: every request waiting at t = 0
+    wall = server.run(reqs, realtime=False)
+    serve_tp = total / wall
+    burst_lat = [r.t_done - r.arrival for r in reqs]
+    # the plain drop-in, one solve at a time, same requests in the same order
+    alone_t, max_err = [], 0.0
+    for r in reqs:
+        res, t = serving.solve_alone(r, device, ops)
+        alone_t.append(t)
+        ref = res.double()
+        max_err = max(max_err, float((r.result.double() - ref).norm() / max(ref.norm(), 1e-30)))
+    plain_tp = total / sum(alone_t)
+    # Poisson arrivals at a rate below the server's measured capacity: latency of each request
+    rate = args.load * count / wall
+    reqs2 = serving.make_stream(count, seed=7, rate_hz=rate)
+    wall2 = server.run(reqs2, realtime=True)
+    lat = [r.t_done - r.arrival for r in reqs2]
+    ratio = [l / a for l, a in zip(lat, alone_t)]
+    line = {"metric": "DOF*steps/s of a mixed solve stream (continuous batching vs one solve at a time)",
+            "value": serve_tp, "unit": "DOF*steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32/c64", "data": "synthetic (seeded band-limited fields)",
+            "config": {"workload": f"serving_{count}_requests", "chunk_steps": args.chunk,
+                       "mix": "KS 1D L=32pi N in {256..4096} | 2D Burgers nu=0.01 N in {64,128,256}; batch 1-32; "
+                              "steps 100-2000; dt 0.01-0.1; ICs |k|<=8, RMS 1 (KS) / 0.25 (Burgers)"},
+            "serving": {"throughput_serve": serve_tp, "throughput_plain": plain_tp,
+                        "speedup_vs_plain": serve_tp / plain_tp,
+                        "burst_latency_s": {"p50": _pctl(burst_lat, 50), "p99": _pctl(burst_lat, 99)},
+                        "poisson_rate_hz": rate, "poisson_wall_s": wall2,
+                        "latency_s": {"p50": _pctl(lat, 50), "p99": _pctl(lat, 99)},
+                        "isolated_latency_s": {"p50": _pctl(alone_t, 50), "p99": _pctl(alone_t, 99)},
+                        "latency_over_isolated": {"p50": _pctl(ratio, 50), "p99": _pctl(ratio, 99)},
+                        "max_rel_diff_mix_vs_alone": max_err},
+            "gpu_launches": server.launches,
+            "e2e": {"value": serve_tp, "unit": "DOF*steps/s",
+                    "h2d_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs),
+                    "d2h_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs)}}
+    print(json.dumps(line))
+
+
+def ncu_case(workload: str = "ns2d"):
+    """Small profiling runs. ns2d: full batch (inputs larger than L2), 3 SETDRK4 steps, 25 launches
+    after a 9-launch warm-up. burgers3d: 256^3 x 3, 1 warm-up step then 2 steps."""
+    import torch
+
+    import __graft_entry__ as entry
+
+    entry.build()
+    from torchfsm_gb300 import initial, pde
+
+    if workload == "burgers3d":
+        n = 256
+        device = torch.device("cuda", 0)
+        u0 = torch.tensor(initial.gaussian_random_field((n, n, n), 1, 3, initial.velocity_spectrum, SEED)
+                          .astype(np.float32), device=device)
+        op = pde.Burgers(0.005)
+        op.integrate(u_0=u0, mesh=[(0.0, 2 * math.pi, n)] * 3, dt=1e-3, step=1)
+        out = op.integrate(u_0=u0, dt=1e-3, step=2)
+        torch.cuda.synchronize()
+        print("ncu case done", bool(torch.isfinite(out).all().item()))
+        return
 
     device = torch.device("cuda", 0)
     u = torch.tensor(initial_vorticity(BATCH), device=device)
@@ -294,11 +499,26 @@ def main():
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=16)
     ap.add_argument("--cpu-time-steps", type=int, default=5)
+    ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
+    ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
+    ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
+    ap.add_argument("--workload", default="ns2d", choices=["ns2d", "burgers1d", "burgers3d", "serving"],
+                    help="ns2d: the headline (2D NS vorticity 256^2 x 64); burgers1d: 1D Burgers N=128 latency; "
+                         "burgers3d: 3D Burgers 256^3")
     ap.add_argument("--ncu-case", action="store_true",
                     help="small profiling case: one warm-up step, then 3 time steps of the full batch")
     args = ap.parse_args()
     if args.ncu_case:
-        ncu_case()
+        ncu_case(args.workload)
+        return
+    if args.workload == "burgers1d" and args.impl == "fused":
+        run_burgers1d(args)
+        return
+    if args.workload == "burgers3d" and args.impl == "fused":
+        run_burgers3d(args)
+        return
+    if args.workload == "serving" and args.impl == "fused":
+        run_serving(args)
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -97,6 +97,9 @@ typedef struct FsmProgramDesc {
   const void* source;            /* DEVICE complex64 [src_batch][n_channel][S], added to the
                                     nonlinear value of every stage; NULL for none */
   int32_t src_batch;             /* 1 or the batch size */
+  int32_t table_batch;           /* entries of the coefficient tables along the batch (0: lin_batch);
+                                    above 1, sample b uses entry b, whose time step can be changed with
+                                    fsm_plan_set_batch_dt (one plan serving samples of different dt) */
 } FsmProgramDesc;
 
 /* Build a plan: validates the program, copies the wavenumbers, masks and
@@ -106,6 +109,17 @@ typedef struct FsmProgramDesc {
  * and may be freed once the stream has passed this call. */
 int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* program, double dt, void* stream,
                     FsmPlan** out);
+
+/* Recompute the coefficient tables of batch entry b for time step dt
+ * (plans with table_batch > 1). Mutates the plan: not to be called while
+ * work using the plan is in flight on another stream. Used by the serving
+ * loop to admit a request with its own dt into a slot. No counterpart in the
+ * reference (its integrator holds one dt, integrator/_stable_etdrk/_uncached.py:180-211). */
+int fsm_plan_set_batch_dt(FsmPlan* plan, int32_t b, double dt, void* stream);
+
+/* Copy the coefficient tables of batch entry src to entry dst (slot
+ * compaction in the serving loop). Same mutation rule as fsm_plan_set_batch_dt. */
+int fsm_plan_move_batch(FsmPlan* plan, int32_t dst, int32_t src, void* stream);
 
 /* Release a plan (synchronises the device first). */
 int fsm_plan_destroy(FsmPlan* plan);

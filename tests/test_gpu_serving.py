@@ -1,0 +1,32 @@
+"""Serving loop: every request's result is the same alone (plain integrate) and in the mix."""
+
+import pytest
+import torch
+
+from torchfsm_gb300 import serving
+
+pytestmark = pytest.mark.gpu
+
+
+def test_results_same_alone_and_in_the_mix():
+    device = torch.device("cuda", 0)
+    reqs = serving.make_stream(14, seed=3, rate_hz=0.0, max_steps=150, min_steps=20)
+    server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=17)
+    server.run(reqs, realtime=False)
+    ops = {}
+    for r in reqs:
+        alone, _ = serving.solve_alone(r, device, ops)
+        assert r.result.shape == alone.shape
+        err = float((r.result.double() - alone.double()).norm() / alone.double().norm())
+        assert err <= 1e-6, f"request {r.rid} ({r.kind} N={r.n} B={r.batch}): {err:.2e}"
+        assert torch.isfinite(r.result).all()
+
+
+def test_admission_respects_capacity_and_compacts():
+    device = torch.device("cuda", 0)
+    reqs = [r for r in serving.make_stream(40, seed=5, rate_hz=0.0, max_steps=60, min_steps=10) if r.kind == "ks1d"]
+    server = serving.SolveServer(device, hbm_budget_bytes=1 << 20, chunk=9, max_slots=40)
+    server.run(reqs, realtime=False)
+    for b in server.buckets.values():
+        assert b.n_active == 0 and all(o is None for o in b.owner)
+    assert all(r.result is not None and r.t_done >= r.t_admit for r in reqs)

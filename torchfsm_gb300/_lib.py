@@ -44,6 +44,8 @@ FSM_SETDRK4 = 14
 EXPORTS = (
     "fsm_plan_create",
     "fsm_plan_destroy",
+    "fsm_plan_set_batch_dt",
+    "fsm_plan_move_batch",
     "fsm_plan_workspace_bytes",
     "fsm_plan_launch_count",
     "fsm_integrate",
@@ -88,6 +90,7 @@ class FsmProgramDesc(ctypes.Structure):
         ("lin_channel", ctypes.c_int32),
         ("source", ctypes.c_void_p),
         ("src_batch", ctypes.c_int32),
+        ("table_batch", ctypes.c_int32),
     ]
 
 
@@ -116,6 +119,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_plan_create.argtypes = [ctypes.POINTER(FsmMeshDesc), ctypes.POINTER(FsmProgramDesc), ctypes.c_double, vp,
                                         ctypes.POINTER(vp)]
         lib.fsm_plan_destroy.argtypes = [vp]
+        lib.fsm_plan_set_batch_dt.argtypes = [vp, i32, ctypes.c_double, vp]
+        lib.fsm_plan_move_batch.argtypes = [vp, i32, i32, vp]
         lib.fsm_plan_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
         lib.fsm_plan_launch_count.argtypes = [vp, i32, ctypes.POINTER(i64)]
         lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]

@@ -164,7 +164,7 @@ class NativePlan:
 
     def __init__(self, program: SpectralProgram, dt: float, integrator: int, device: torch.device,
                  n_integration_points: int = 16, integration_radius: float = 1.0,
-                 linear_coef64: Optional[torch.Tensor] = None):
+                 linear_coef64: Optional[torch.Tensor] = None, table_batch: int = 0):
         self.program = program
         self.dt = float(dt)
         self.integrator = integrator
@@ -214,6 +214,8 @@ class NativePlan:
         else:
             desc.lin_batch = 1
             desc.lin_channel = 1
+        desc.table_batch = int(table_batch)
+        self.table_batch = int(table_batch)
         self.src_batch = 0
         self._src_half = None
         handle = ctypes.c_void_p()
@@ -248,6 +250,14 @@ class NativePlan:
             except Exception:
                 pass
             self.handle = None
+
+    def set_batch_dt(self, b: int, dt: float) -> None:
+        """Recompute the tables of batch entry b for time step dt (plans built with table_batch > 1)."""
+        _lib.check(_lib.load().fsm_plan_set_batch_dt(self.handle, int(b), float(dt), _stream(self.device)))
+
+    def move_batch(self, dst: int, src: int) -> None:
+        """Copy the tables of batch entry src to entry dst."""
+        _lib.check(_lib.load().fsm_plan_move_batch(self.handle, int(dst), int(src), _stream(self.device)))
 
     def workspace_bytes(self, batch: int, steps: int) -> int:
         out = ctypes.c_size_t()

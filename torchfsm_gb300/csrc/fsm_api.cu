@@ -59,11 +59,14 @@ __device__ __forceinline__ float2 tof(cd z) { return make_float2((float)z.x, (fl
 // SETDRK: phi-functions as the mean over M contour points z_j = r e^{i pi (2j-1)/M} + dt L
 // of the Kassam-Trefethen integrands, real part kept (integrator/_stable_etdrk/_uncached.py:8-43, 46-211);
 // ETDRK1/2: closed forms with the L == 0 limits (integrator/_etdrk.py:30-82).
-__global__ void k_phi_tables(const double2* __restrict__ L, int64_t count, double dt, int integ, int M, double r,
-                             float2* __restrict__ tab, int64_t ts) {
-  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= count) return;
-  const cd l = L ? mk(L[idx].x, L[idx].y) : mk(0.0, 0.0);
+// `count` entries starting at table entry offset `first`; L is indexed modulo `lcount`
+// (L shared by every table entry when the symbol has no batch dimension).
+__global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int64_t first, int64_t count, double dt,
+                             int integ, int M, double r, float2* __restrict__ tab, int64_t ts) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int64_t idx = first + k;
+  const cd l = L ? mk(L[idx % lcount].x, L[idx % lcount].y) : mk(0.0, 0.0);
   const cd hl = dt * l;
   const cd E = cexpd(hl);
   tab[idx] = tof(E);
@@ -173,6 +176,7 @@ static void free_plan(FsmPlan* p) {
   cudaFree(p->tw);
   cudaFree(p->tab);
   cudaFree(p->source);
+  cudaFree(p->lin);
   delete p;
 }
 
@@ -269,8 +273,17 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
   p->nstages = scheme_stages(integ);
   p->ntab = scheme_tables(integ);
   p->nl_coef = (float)prog->nonlinear_coef;
-  p->lin_batch = prog->linear_coef ? prog->lin_batch : 1;
+  p->lin_src_batch = prog->linear_coef ? prog->lin_batch : 1;
   p->lin_ch = prog->linear_coef ? prog->lin_channel : 1;
+  p->lin_batch = prog->table_batch > 0 ? prog->table_batch : p->lin_src_batch;
+  if (p->lin_src_batch > 1 && p->lin_batch != p->lin_src_batch) {
+    delete p;
+    return set_error(FSM_ERR_INVALID, "table_batch must equal lin_batch for a batched linear coefficient");
+  }
+  p->lin_present = prog->linear_coef != nullptr;
+  p->dt = dt;
+  p->n_points = prog->n_integration_points > 0 ? prog->n_integration_points : 16;
+  p->radius = prog->integration_radius > 0 ? prog->integration_radius : 1.0;
   p->path = path;
   p->n_aux = scheme_aux(integ);
   if (path == 2) {
@@ -328,12 +341,20 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       return rc;
     }
   }
+  const int64_t lcount = (int64_t)p->lin_src_batch * p->lin_ch * p->S;
+  if (p->lin_present) {
+    // keep the FP64 symbol for later per-entry time-step changes
+    if ((rc = cuda_check(cudaMalloc(&p->lin, lcount * sizeof(double2)), "cudaMalloc linear symbol")) ||
+        (rc = cuda_check(cudaMemcpyAsync(p->lin, prog->linear_coef, lcount * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                         st), "copy linear symbol"))) {
+      free_plan(p);
+      return rc;
+    }
+  }
   const int64_t count = p->tstride;
   const int threads = 128;
   k_phi_tables<<<(unsigned)((count + threads - 1) / threads), threads, 0, st>>>(
-      (const double2*)prog->linear_coef, count, dt, integ,
-      prog->n_integration_points > 0 ? prog->n_integration_points : 16,
-      prog->integration_radius > 0 ? prog->integration_radius : 1.0, p->tab, p->tstride);
+      p->lin, lcount, 0, count, dt, integ, p->n_points, p->radius, p->tab, p->tstride);
   if ((rc = cuda_check(cudaGetLastError(), "k_phi_tables"))) {
     free_plan(p);
     return rc;
@@ -344,6 +365,30 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
     return rc;
   }
   *out = p;
+  return FSM_OK;
+}
+
+int fsm_plan_set_batch_dt(FsmPlan* p, int32_t b, double dt, void* stream) {
+  if (!p || b < 0 || b >= p->lin_batch || p->lin_batch < 2) return set_error(FSM_ERR_INVALID, "set_batch_dt arguments");
+  const int64_t per = (int64_t)p->lin_ch * p->S;
+  const int64_t lcount = (int64_t)p->lin_src_batch * per;
+  const int threads = 128;
+  k_phi_tables<<<(unsigned)((per + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
+      p->lin, lcount, (int64_t)b * per, per, dt, p->integ, p->n_points, p->radius, p->tab, p->tstride);
+  return cuda_check(cudaGetLastError(), "k_phi_tables (batch entry)");
+}
+
+int fsm_plan_move_batch(FsmPlan* p, int32_t dst, int32_t src, void* stream) {
+  if (!p || dst < 0 || src < 0 || dst >= p->lin_batch || src >= p->lin_batch)
+    return set_error(FSM_ERR_INVALID, "move_batch arguments");
+  if (dst == src) return FSM_OK;
+  const int64_t per = (int64_t)p->lin_ch * p->S;
+  for (int t = 0; t < p->ntab; ++t) {
+    int rc = cuda_check(cudaMemcpyAsync(p->tab + t * p->tstride + dst * per, p->tab + t * p->tstride + src * per,
+                                        per * sizeof(float2), cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                        "move tables");
+    if (rc) return rc;
+  }
   return FSM_OK;
 }
 
@@ -451,7 +496,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   const size_t need = workspace_layout(p, batch, steps, &off_arrays);
   if (!workspace || workspace_bytes < need)
     return set_error(FSM_ERR_INVALID, "workspace too small: need " + std::to_string(need) + " bytes");
-  if (p->lin_batch > 1 && p->lin_batch != batch) return set_error(FSM_ERR_INVALID, "batch != lin_batch");
+  if (p->lin_batch > 1 && batch > p->lin_batch) return set_error(FSM_ERR_INVALID, "batch above the plan's table entries");
   if (p->source && p->src_batch > 1 && p->src_batch != batch) return set_error(FSM_ERR_INVALID, "batch != src_batch");
   if ((int64_t)batch * p->C > 65535 && p->path == 2) return set_error(FSM_ERR_UNSUPPORTED, "batch too large for one launch");
   if (p->path == 4 && (int64_t)batch * p->n_prod * p->n[0] > 65535)

@@ -171,6 +171,12 @@ struct FsmPlan {
   float2* tab = nullptr;     // [ntab][lin_batch][lin_ch][S]
   int64_t tstride = 0;       // lin_batch * lin_ch * S
   float2* source = nullptr;  // [src_batch][C][S] or null
+  double2* lin = nullptr;    // FP64 linear symbol [lin_src_batch][lin_ch][S] kept for per-entry dt changes
+  int lin_src_batch = 1;
+  int lin_present = 0;
+  double dt = 0.0;
+  int n_points = 16;
+  double radius = 1.0;
   // fused-path array counts per sample (2D / 3D)
   int n_mid = 0, n_prod = 0, n_aux = 0, n_mid2 = 0;
   int path = 0;  // 1: line kernel (1D), 2: plane passes (2D), 3: pointwise, 4: volume passes (3D)

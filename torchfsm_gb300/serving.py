@@ -1,0 +1,270 @@
+"""Continuous-batching solve server on one GPU.
+
+Requests (PDE kind, grid size, batch, step count, dt, initial field) arrive
+over time. Requests of the same kind and grid size share a *bucket*: one
+plan whose coefficient tables have one entry per slot (each slot carries its
+own dt, set with ``fsm_plan_set_batch_dt``), one slot-batched spectral state
+and one workspace, sized at start-up from an HBM budget. Every *tick*
+advances all active slots of a bucket by up to ``chunk`` steps in one fused
+launch sequence (2D: one column + one row pass launch per stage for all
+slots; 1D: one launch); buckets tick on their own streams, so their work
+overlaps on the device. Between ticks finished requests leave (their slots
+are transformed back and copied to the host), the remaining slots are
+compacted, and waiting requests are admitted while slots are free.
+
+Per-sample arithmetic is independent of the other samples in the launch,
+so a request's result is the same alone and in the mix.
+
+The reference has no serving layer; the solves themselves follow
+``Operator.integrate`` (operator/_base.py:676-751) for
+``KuramotoSivashinsky()`` (pde.py:27-39) and ``Burgers(nu)`` (pde.py:13-25).
+"""
+
+from __future__ import annotations
+
+import collections
+import math
+import time
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib, _native, pde
+from .mesh import FourierMesh
+
+KS_LENGTH = 32 * math.pi
+BURGERS_NU = 0.01
+
+
+@dataclass
+class SolveRequest:
+    rid: int
+    kind: str            # "ks1d" | "burgers2d"
+    n: int
+    batch: int
+    steps: int
+    dt: float
+    u0: torch.Tensor     # host float32 [batch, C, *shape]
+    arrival: float = 0.0
+    t_admit: Optional[float] = None
+    t_done: Optional[float] = None
+    result: Optional[torch.Tensor] = None
+    remaining: int = 0
+    slots: List[int] = field(default_factory=list)
+
+    @property
+    def dof_steps(self) -> int:
+        return int(np.prod(self.u0.shape)) * self.steps
+
+
+def problem(kind: str, n: int):
+    """(operator, mesh_info, channels) of a request kind."""
+    if kind == "ks1d":
+        return pde.KuramotoSivashinsky(), [(0.0, KS_LENGTH, n)], 1
+    if kind == "burgers2d":
+        return pde.Burgers(BURGERS_NU), [(0.0, 2 * math.pi, n), (0.0, 2 * math.pi, n)], 2
+    raise ValueError(kind)
+
+
+def slot_bytes(kind: str, n: int, chunk: int) -> int:
+    """HBM per slot: state + workspace + coefficient tables."""
+    _, mesh, C = problem(kind, n)
+    shape = [m[2] for m in mesh]
+    S = int(np.prod(shape[:-1])) * (shape[-1] // 2 + 1)
+    per_field = S * 8
+    if kind == "ks1d":
+        return per_field * (C + 6)
+    return per_field * (C + 2 * C + 4 + C + 6)
+
+
+class _Bucket:
+    def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int):
+        self.kind, self.n, self.capacity, self.device, self.chunk = kind, n, capacity, device, chunk
+        op, mesh, C = problem(kind, n)
+        self.C = C
+        f_mesh = FourierMesh(mesh, device=device, dtype=torch.float32)
+        op.register_mesh(f_mesh, C)
+        prog = _native.lower(op._linear_terms, op._nonlinear_funcs, f_mesh, C, op._de_aliasing_rate)
+        self.stream = torch.cuda.Stream(device)
+        with torch.cuda.stream(self.stream):
+            self.plan = _native.NativePlan(prog, 0.05, _lib.FSM_SETDRK4, device,
+                                           linear_coef64=op._linear_coef64(device), table_batch=capacity)
+            self.sp = _native.Spectral(self.plan)
+            half = tuple(m[2] for m in mesh[:-1]) + (mesh[-1][2] // 2 + 1,)
+            self.state = torch.empty((capacity, C) + half, dtype=torch.complex64, device=device)
+            self.ws = torch.empty(self.plan.workspace_bytes(capacity, chunk), dtype=torch.uint8, device=device)
+        self.owner: List[Optional[Tuple[SolveRequest, int]]] = [None] * capacity
+        self.active: List[SolveRequest] = []
+        self.n_active = 0
+        self.tick: Optional[Tuple[torch.cuda.Event, int]] = None
+        self.launches = 0
+
+    def can_admit(self, req: SolveRequest) -> bool:
+        return self.tick is None and self.capacity - self.n_active >= req.batch
+
+    def admit(self, req: SolveRequest, now: float) -> None:
+        with torch.cuda.stream(self.stream):
+            u = req.u0.to(self.device, non_blocking=True)
+            half = self.sp.to_half(u)
+            lo = self.n_active
+            self.state[lo:lo + req.batch].copy_(half)
+            for i in range(req.batch):
+                self.plan.set_batch_dt(lo + i, req.dt)
+                self.owner[lo + i] = (req, i)
+        req.slots = list(range(lo, lo + req.batch))
+        req.remaining = req.steps
+        req.t_admit = now
+        self.active.append(req)
+        self.n_active += req.batch
+
+    def launch(self) -> None:
+        k = min(self.chunk, min(r.remaining for r in self.active))
+        with torch.cuda.stream(self.stream):
+            self.plan.integrate_half(self.state[: self.n_active], k, workspace=self.ws)
+            ev = torch.cuda.Event()
+            ev.record(self.stream)
+        self.launches += self.plan.launch_count(k)
+        self.tick = (ev, k)
+
+    def poll(self, now_fn) -> List[SolveRequest]:
+        """Finish the tick if the device is done with it; return the requests that completed."""
+        if self.tick is None or not self.tick[0].query():
+            return []
+        k = self.tick[1]
+        self.tick = None
+        done = []
+        for r in self.active:
+            r.remaining -= k
+            if r.remaining == 0:
+                done.append(r)
+        if not done:
+            return []
+        with torch.cuda.stream(self.stream):
+            for r in done:
+                idx = torch.tensor(r.slots, device=self.device)
+                out = self.sp.to_physical(self.state.index_select(0, idx), keep_input=False)
+                r.result = out.to("cpu")
+            self.stream.synchronize()
+        t = now_fn()
+        for r in done:
+            r.t_done = t
+            for s in r.slots:
+                self.owner[s] = None
+        self.active = [r for r in self.active if r.remaining > 0]
+        self._compact()
+        return done
+
+    def _compact(self) -> None:
+        """Move the highest occupied slots into freed holes so that slots [0, n_active) are occupied."""
+        occupied = [i for i in range(self.capacity) if self.owner[i] is not None]
+        n = len(occupied)
+        holes = [i for i in range(n) if self.owner[i] is None]
+        movers = [i for i in occupied if i >= n]
+        with torch.cuda.stream(self.stream):
+            for h, m in zip(holes, movers):
+                self.state[h].copy_(self.state[m])
+                self.plan.move_batch(h, m)
+                req, i = self.owner[m]
+                req.slots[i] = h
+                self.owner[h] = (req, i)
+                self.owner[m] = None
+        self.n_active = n
+
+
+class SolveServer:
+    """Admission by HBM budget, per-bucket ticks on separate streams."""
+
+    def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
+                 max_slots: int = 256):
+        self.device = device
+        self.budget = hbm_budget_bytes
+        self.chunk = chunk
+        self.max_slots = max_slots
+        self.buckets: Dict[Tuple[str, int], _Bucket] = {}
+
+    def prepare(self, keys: List[Tuple[str, int]], max_batch: int = 32) -> None:
+        """Create one bucket per (kind, n), splitting the HBM budget by footprint."""
+        share = self.budget // max(1, len(keys))
+        for kind, n in keys:
+            cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
+            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk)
+        torch.cuda.synchronize(self.device)
+
+    def run(self, requests: List[SolveRequest], realtime: bool = True) -> float:
+        """Serve the requests (arrival times in seconds from start); returns the wall time."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        keys = sorted({(r.kind, r.n) for r in pending})
+        missing = [k for k in keys if k not in self.buckets]
+        if missing:
+            self.prepare(missing)
+        waiting: Dict[Tuple[str, int], collections.deque] = {k: collections.deque() for k in self.buckets}
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        i, finished, total = 0, 0, len(pending)
+        while finished < total:
+            t = now()
+            while i < total and (not realtime or pending[i].arrival <= t):
+                waiting[(pending[i].kind, pending[i].n)].append(pending[i])
+                i += 1
+            busy = False
+            for key, b in self.buckets.items():
+                finished += len(b.poll(now))
+                if b.tick is None:
+                    q = waiting[key]
+                    while q and b.can_admit(q[0]):
+                        b.admit(q.popleft(), now())
+                    if b.n_active:
+                        b.launch()
+                if b.tick is not None:
+                    busy = True
+            if not busy:
+                time.sleep(0.0001)
+        return now()
+
+    @property
+    def launches(self) -> int:
+        return sum(b.launches for b in self.buckets.values())
+
+
+def make_stream(count: int, seed: int, rate_hz: float, max_steps: int = 2000, min_steps: int = 100,
+                kmax: int = 8) -> List[SolveRequest]:
+    """The mixed request stream: uniform over {KS 1D, N in 256..4096; 2D Burgers, N in 64..256},
+    batch 1-32, steps 100-2000, dt 0.01-0.1, band-limited N(0,1) initial fields (|k| <= 8) scaled to
+    RMS 1 (KS) / 0.25 (Burgers: unit RMS diverges at dt >= 0.02 in the reference), Poisson arrivals."""
+    from . import initial
+
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for rid in range(count):
+        t += rng.exponential(1.0 / rate_hz) if rate_hz > 0 else 0.0
+        if rng.integers(0, 2) == 0:
+            kind, n, rms = "ks1d", int(rng.choice([256, 512, 1024, 2048, 4096])), 1.0
+            shape = (n,)
+            C = 1
+        else:
+            kind, n, rms = "burgers2d", int(rng.choice([64, 128, 256])), 0.25
+            shape = (n, n)
+            C = 2
+        batch = int(rng.integers(1, 33))
+        steps = int(rng.integers(min_steps, max_steps + 1))
+        dt = float(rng.uniform(0.01, 0.1))
+        u0 = initial.band_limited(shape, batch, C, kmax, int(rng.integers(0, 2 ** 31)), rms).astype(np.float32)
+        out.append(SolveRequest(rid, kind, n, batch, steps, dt, torch.from_numpy(u0), arrival=t))
+    return out
+
+
+def solve_alone(req: SolveRequest, device: torch.device, ops: Dict) -> Tuple[torch.Tensor, float]:
+    """The plain drop-in: one ``integrate`` call for the request, result copied to the host."""
+    key = (req.kind, req.n)
+    if key not in ops:
+        ops[key] = problem(req.kind, req.n)
+    op, mesh, _ = ops[key]
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    u = req.u0.to(device)
+    out = op.integrate(u_0=u, mesh=mesh if op._state_dict["f_mesh"] is None else None, dt=req.dt, step=req.steps)
+    res = out.cpu()
+    return res, time.perf_counter() - t0

@@ -231,3 +231,21 @@ def namespace(module_root):
         traj_recorder=importlib.import_module(module_root + ".traj_recorder"),
         torch=torch,
     )
+
+
+# Differentiable workloads: loss = MSE(u_T(u0, nu), target), target from the same u0 with nu_target.
+GRAD_CASES = {
+    "grad_burgers2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=2, dt=0.005, step=20,
+        nu=0.01, nu_target=0.02, ic=_bl(151, (32, 32), 4, 1.0),
+    ),
+    "grad_burgers1d_n64": dict(
+        mesh=[(0, TWO_PI, 64)], batch=3, channels=1, dt=0.01, step=30,
+        nu=0.05, nu_target=0.1, ic=_bl(161, (64,), 5, 1.0),
+    ),
+}
+
+
+def grad_initial_condition(name: str) -> np.ndarray:
+    c = GRAD_CASES[name]
+    return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)

@@ -82,6 +82,24 @@ def main(ref_root: str) -> None:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
         print(name, payload["final"].shape, payload["integrator"])
 
+    # Gradients by the reference's own autograd (float64): d loss / d u0, d loss / d nu.
+    for name, case in C.GRAD_CASES.items():
+        if only and name not in only:
+            continue
+        u0 = torch.tensor(C.grad_initial_condition(name), dtype=torch.float64)
+        with torch.no_grad():
+            target = M.pde.Burgers(case["nu_target"]).integrate(u_0=u0, mesh=case["mesh"], dt=case["dt"],
+                                                                 step=case["step"])
+        nu = torch.tensor(case["nu"], dtype=torch.float64, requires_grad=True)
+        x = u0.clone().requires_grad_(True)
+        op = nu * M.operator.Laplacian() - M.operator.Convection()
+        out = op.integrate(u_0=x, mesh=case["mesh"], dt=case["dt"], step=case["step"])
+        loss = ((out - target) ** 2).mean()
+        loss.backward()
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), u0=u0.numpy(), target=target.numpy(),
+                            loss=np.array(loss.item()), grad_u0=x.grad.numpy(), grad_nu=np.array(nu.grad.item()))
+        print(name, "loss", loss.item(), "grad_nu", nu.grad.item())
+
     if only:
         return
     # Coefficient tables (integrator/_stable_etdrk/_uncached.py:180-211, _etdrk.py:54-82).

@@ -327,6 +327,7 @@ class OperatorLike(_MutableMixIn):
                                       "use an ETDRKIntegrator or SETDRKIntegrator")
         return int(self._integrator.value)
 
+    @torch.no_grad()
     def _build_integrator(self, dt: float, device: torch.device):
         if not self._linear_terms and not self._nonlinear_funcs:
             raise ValueError("Both linear coefficient and nonlinear function are None. Cannot build operator.")
@@ -378,6 +379,15 @@ class OperatorLike(_MutableMixIn):
             integ = self._state_dict["integrator"]
         real_dtype = value.dtype if not value.is_complex() else value.real.dtype
         _native.warn_precision(real_dtype)
+        needs_grad = torch.is_grad_enabled() and (
+            (u_0 is not None and u_0.requires_grad)
+            or any(isinstance(c, Tensor) and c.requires_grad for c, _ in self._linear_terms))
+        if needs_grad:
+            if trajectory_recorder is not None or return_in_fourier or u_0 is None:
+                raise NotImplementedError("gradients are provided for integrate(u_0, ...) returning the final field")
+            from ..adjoint import integrate_with_grad
+
+            return integrate_with_grad(self, u_0, dt, int(step)).to(real_dtype)
         sp = integ.spectral
         if u_0_fft is None:
             state = sp.to_half(u_0)

@@ -489,7 +489,8 @@ def run_burgers2d_grad(args):
         u = u0d.clone().requires_grad_(True)
         out = op.integrate(u_0=u, dt=dt, step=steps)
         loss = ((out - target) ** 2).mean()
-        loss.backward()
+        # the operator's coefficient is the non-leaf tensor 1 * nu, shared by every call
+        loss.backward(retain_graph=True)
         return loss.item(), u.grad, nu.grad.item()
 
     for _ in range(max(1, args.warmup)):

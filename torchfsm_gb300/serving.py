@@ -80,14 +80,17 @@ def slot_bytes(kind: str, n: int, chunk: int) -> int:
 
 
 class _Bucket:
-    def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int):
+    def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int,
+                 priority: int = 0, tick_ms: float = 4.0):
         self.kind, self.n, self.capacity, self.device, self.chunk = kind, n, capacity, device, chunk
+        self.tick_ms = tick_ms
+        self.step_ms: Optional[float] = None  # measured device time per step and slot
         op, mesh, C = problem(kind, n)
         self.C = C
         f_mesh = FourierMesh(mesh, device=device, dtype=torch.float32)
         op.register_mesh(f_mesh, C)
         prog = _native.lower(op._linear_terms, op._nonlinear_funcs, f_mesh, C, op._de_aliasing_rate)
-        self.stream = torch.cuda.Stream(device)
+        self.stream = torch.cuda.Stream(device, priority=priority)
         with torch.cuda.stream(self.stream):
             self.plan = _native.NativePlan(prog, 0.05, _lib.FSM_SETDRK4, device,
                                            linear_coef64=op._linear_coef64(device), table_batch=capacity)
@@ -98,7 +101,7 @@ class _Bucket:
         self.owner: List[Optional[Tuple[SolveRequest, int]]] = [None] * capacity
         self.active: List[SolveRequest] = []
         self.n_active = 0
-        self.tick: Optional[Tuple[torch.cuda.Event, int]] = None
+        self.tick: Optional[Tuple[torch.cuda.Event, torch.cuda.Event, int, int]] = None
         self.launches = 0
 
     def can_admit(self, req: SolveRequest) -> bool:
@@ -121,19 +124,27 @@ class _Bucket:
 
     def launch(self) -> None:
         k = min(self.chunk, min(r.remaining for r in self.active))
+        if self.step_ms:
+            # ticks of about tick_ms of device work keep admission and small requests responsive
+            k = max(1, min(k, int(self.tick_ms / (self.step_ms * self.n_active))))
         with torch.cuda.stream(self.stream):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
             self.plan.integrate_half(self.state[: self.n_active], k, workspace=self.ws)
-            ev = torch.cuda.Event()
-            ev.record(self.stream)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e1.record(self.stream)
         self.launches += self.plan.launch_count(k)
-        self.tick = (ev, k)
+        self.tick = (e0, e1, k, self.n_active)
 
-    def poll(self, now_fn) -> List[SolveRequest]:
-        """Finish the tick if the device is done with it; return the requests that completed."""
-        if self.tick is None or not self.tick[0].query():
+    def poll(self) -> List[SolveRequest]:
+        """Finish the tick if the device is done with it; return the requests that completed, whose
+        results are being copied to pinned host memory (``r._copied`` records when)."""
+        if self.tick is None or not self.tick[1].query():
             return []
-        k = self.tick[1]
+        e0, e1, k, n = self.tick
         self.tick = None
+        ms = e0.elapsed_time(e1) / (k * n)
+        self.step_ms = ms if self.step_ms is None else 0.5 * (self.step_ms + ms)
         done = []
         for r in self.active:
             r.remaining -= k
@@ -145,11 +156,11 @@ class _Bucket:
             for r in done:
                 idx = torch.tensor(r.slots, device=self.device)
                 out = self.sp.to_physical(self.state.index_select(0, idx), keep_input=False)
-                r.result = out.to("cpu")
-            self.stream.synchronize()
-        t = now_fn()
+                r.result = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+                r.result.copy_(out, non_blocking=True)
+                r._copied = torch.cuda.Event()
+                r._copied.record(self.stream)
         for r in done:
-            r.t_done = t
             for s in r.slots:
                 self.owner[s] = None
         self.active = [r for r in self.active if r.remaining > 0]
@@ -177,19 +188,23 @@ class SolveServer:
     """Admission by HBM budget, per-bucket ticks on separate streams."""
 
     def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
-                 max_slots: int = 256):
+                 max_slots: int = 256, tick_ms: float = 4.0):
         self.device = device
         self.budget = hbm_budget_bytes
         self.chunk = chunk
         self.max_slots = max_slots
+        self.tick_ms = tick_ms
         self.buckets: Dict[Tuple[str, int], _Bucket] = {}
 
     def prepare(self, keys: List[Tuple[str, int]], max_batch: int = 32) -> None:
         """Create one bucket per (kind, n), splitting the HBM budget by footprint."""
         share = self.budget // max(1, len(keys))
+        lo, hi = torch.cuda.Stream.priority_range()
         for kind, n in keys:
             cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
-            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk)
+            # cheap per-step buckets (1D, small 2D grids) get the higher-priority streams
+            prio = hi if (kind == "ks1d" or n <= 64) else lo
+            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms)
         torch.cuda.synchronize(self.device)
 
     def run(self, requests: List[SolveRequest], realtime: bool = True) -> float:
@@ -203,14 +218,23 @@ class SolveServer:
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
         i, finished, total = 0, 0, len(pending)
+        copying: List[SolveRequest] = []
         while finished < total:
             t = now()
             while i < total and (not realtime or pending[i].arrival <= t):
                 waiting[(pending[i].kind, pending[i].n)].append(pending[i])
                 i += 1
-            busy = False
+            busy = bool(copying)
+            still = []
+            for r in copying:
+                if r._copied.query():
+                    r.t_done = now()
+                    finished += 1
+                else:
+                    still.append(r)
+            copying = still
             for key, b in self.buckets.items():
-                finished += len(b.poll(now))
+                copying.extend(b.poll())
                 if b.tick is None:
                     q = waiting[key]
                     while q and b.can_admit(q[0]):

@@ -59,6 +59,22 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def max_over_ranks(value: float, dist, device=None) -> float:
+    """Max of a per-rank value over all ranks (the slowest rank's time); identity without dist."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: float, world: int, ms_max: float) -> float:
+    """Whole-job throughput: the units of all ranks over the slowest rank's time (weak scaling)."""
+    return world * units_per_rank / (ms_max * 1e-3)
+
+
 def initial_vorticity(batch: int, seed: int = SEED) -> np.ndarray:
     from torchfsm_gb300 import initial
 
@@ -192,11 +208,7 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
     torch.cuda.synchronize()
     if dist is not None:
         dist.barrier()
-    ms = sum(times) / len(times)
-    if dist is not None:
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(sum(times) / len(times), dist, device)
     finite = bool(torch.isfinite(torch.view_as_real(state)).all().item())
 
     # e2e through the public API with host buffers
@@ -212,11 +224,7 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
         t1 = time.perf_counter()
         if i >= args.warmup:
             e2e_times.append((t1 - t0) * 1e3)
-    e2e_ms = sum(e2e_times) / len(e2e_times)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(sum(e2e_times) / len(e2e_times), dist, device)
 
     # instrumented pass: per-kernel CUDA-event timing of one integration
     prof = profile_kernels(plan, state0, ws, device)
@@ -634,8 +642,8 @@ def main():
             dist.destroy_process_group()
         return
     dof_steps = res["B"] * N * N * TIME_STEPS
-    value = world * dof_steps / (res["ms"] * 1e-3)
-    e2e_value = world * dof_steps / (res["e2e_ms"] * 1e-3)
+    value = job_throughput(dof_steps, world, res["ms"])
+    e2e_value = job_throughput(dof_steps, world, res["e2e_ms"])
     peak, peak_kind = _peaks()
     col = res["prof"]["column_pass"]
     achieved = column_pass_bytes(res["B"]) / (col["avg_ms"] * 1e-3) / 1e9 if col["avg_ms"] else None

@@ -121,6 +121,13 @@ int fsm_plan_set_batch_dt(FsmPlan* plan, int32_t b, double dt, void* stream);
  * compaction in the serving loop). Same mutation rule as fsm_plan_set_batch_dt. */
 int fsm_plan_move_batch(FsmPlan* plan, int32_t dst, int32_t src, void* stream);
 
+/* Copy the plan's coefficient tables (complex64, [ntab][table_batch][lin_channel][S], the
+ * scheme's order: SETDRK4 E, E2, c1, c4, c5, c6) to the device buffer dst of
+ * capacity_bytes; with dst == NULL only report ntab and the entries per table.
+ * Inspection of UnCachedSETDRK*.__init__'s tables (integrator/_stable_etdrk/_uncached.py:180-211). */
+int fsm_plan_tables(const FsmPlan* plan, void* dst, size_t capacity_bytes, int32_t* ntab, int64_t* entries,
+                    void* stream);
+
 /* Release a plan (synchronises the device first). */
 int fsm_plan_destroy(FsmPlan* plan);
 

@@ -46,6 +46,7 @@ EXPORTS = (
     "fsm_plan_destroy",
     "fsm_plan_set_batch_dt",
     "fsm_plan_move_batch",
+    "fsm_plan_tables",
     "fsm_plan_workspace_bytes",
     "fsm_plan_launch_count",
     "fsm_integrate",
@@ -121,6 +122,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_plan_destroy.argtypes = [vp]
         lib.fsm_plan_set_batch_dt.argtypes = [vp, i32, ctypes.c_double, vp]
         lib.fsm_plan_move_batch.argtypes = [vp, i32, i32, vp]
+        lib.fsm_plan_tables.argtypes = [vp, vp, sz, ctypes.POINTER(i32), ctypes.POINTER(i64), vp]
         lib.fsm_plan_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
         lib.fsm_plan_launch_count.argtypes = [vp, i32, ctypes.POINTER(i64)]
         lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]

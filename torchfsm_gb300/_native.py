@@ -251,6 +251,16 @@ class NativePlan:
                 pass
             self.handle = None
 
+    def tables(self) -> torch.Tensor:
+        """The plan's coefficient tables [ntab, table_batch * lin_channel * S] (complex64)."""
+        lib = _lib.load()
+        nt, ne = ctypes.c_int32(), ctypes.c_int64()
+        _lib.check(lib.fsm_plan_tables(self.handle, None, 0, ctypes.byref(nt), ctypes.byref(ne), None))
+        out = torch.empty((nt.value, ne.value), dtype=torch.complex64, device=self.device)
+        _lib.check(lib.fsm_plan_tables(self.handle, out.data_ptr(), out.numel() * 8, None, None,
+                                       _stream(self.device)))
+        return out
+
     def set_batch_dt(self, b: int, dt: float) -> None:
         """Recompute the tables of batch entry b for time step dt (plans built with table_batch > 1)."""
         _lib.check(_lib.load().fsm_plan_set_batch_dt(self.handle, int(b), float(dt), _stream(self.device)))

@@ -132,13 +132,15 @@ class ConvectionAdjoint:
         g = [self._phys(self._ik(i, d)) for i in range(self.nd)]  # g[i][:, c] = d_i u_c
         return u, g
 
-    def nonlinear(self, a):
+    def nonlinear(self, a, keep=None):
         u, g = self._fields(a)
+        if keep is not None:
+            keep.append((u, g))
         p = sum(u[:, i:i + 1] * g[i] for i in range(self.nd))   # p_c = sum_i u_i d_i u_c
         return self.coef * self._spec(p)
 
-    def nonlinear_vjp(self, a, nbar):
-        u, g = self._fields(a)
+    def nonlinear_vjp(self, a, nbar, fields=None):
+        u, g = fields if fields is not None else self._fields(a)
         w = (self.coef * self.ntot) * self._phys(nbar)        # [B, C, ...]
         # ubar_c = sum_c' w_c' d_c u_c'
         ubar = torch.stack([(w * g[c]).sum(1) for c in range(self.nd)], dim=1)
@@ -150,13 +152,14 @@ class ConvectionAdjoint:
     # -- one SETDRK4 step and its adjoint --------------------------------------
     def step_adjoint(self, u, ubar_next, tbar):
         E, E2, c1, c4, c5, c6 = self.tabs
-        n0 = self.nonlinear(u)
+        fl = []  # physical fields of each stage input, reused by the vector-Jacobian products
+        n0 = self.nonlinear(u, fl)
         a1 = E2 * u + c1 * n0
-        n1 = self.nonlinear(a1)
+        n1 = self.nonlinear(a1, fl)
         a2 = E2 * u + c1 * n1
-        n2 = self.nonlinear(a2)
+        n2 = self.nonlinear(a2, fl)
         a3 = E2 * a1 + c1 * (2 * n2 - n0)
-        n3 = self.nonlinear(a3)
+        n3 = self.nonlinear(a3, fl)
 
         def acc(t, x, y):
             if tbar is not None:
@@ -172,23 +175,23 @@ class ConvectionAdjoint:
         acc(4, ub, 2 * (n1 + n2))
         n3b = c6 * ub
         acc(5, ub, n3)
-        a3b = self.nonlinear_vjp(a3, n3b)
+        a3b = self.nonlinear_vjp(a3, n3b, fl[3])
         a1b = E2 * a3b
         acc(1, a3b, a1)
         n2b = n2b + 2 * c1 * a3b
         n0b = n0b - c1 * a3b
         acc(2, a3b, 2 * n2 - n0)
-        a2b = self.nonlinear_vjp(a2, n2b)
+        a2b = self.nonlinear_vjp(a2, n2b, fl[2])
         u_bar = u_bar + E2 * a2b
         acc(1, a2b, u)
         n1b = n1b + c1 * a2b
         acc(2, a2b, n1)
-        a1b = a1b + self.nonlinear_vjp(a1, n1b)
+        a1b = a1b + self.nonlinear_vjp(a1, n1b, fl[1])
         u_bar = u_bar + E2 * a1b
         acc(1, a1b, u)
         n0b = n0b + c1 * a1b
         acc(2, a1b, n0)
-        u_bar = u_bar + self.nonlinear_vjp(u, n0b)
+        u_bar = u_bar + self.nonlinear_vjp(u, n0b, fl[0])
         return u_bar
 
     def coef_gradient(self, tbar, symbol_half: torch.Tensor) -> torch.Tensor:

@@ -4,7 +4,10 @@
 #include <math.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "fsm_internal.cuh"
@@ -22,6 +25,21 @@ int cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return FSM_OK;
   const int code = (e == cudaErrorMemoryAllocation) ? FSM_ERR_OOM : FSM_ERR_CUDA;
   return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+static std::mutex g_attr_mutex;
+static std::map<std::pair<const void*, int>, size_t> g_attr;
+
+bool smem_attr_known(const void* kernel, int device, size_t smem) {
+  std::lock_guard<std::mutex> lock(g_attr_mutex);
+  auto it = g_attr.find({kernel, device});
+  return it != g_attr.end() && it->second >= smem;
+}
+
+void smem_attr_record(const void* kernel, int device, size_t smem) {
+  std::lock_guard<std::mutex> lock(g_attr_mutex);
+  size_t& v = g_attr[{kernel, device}];
+  if (smem > v) v = smem;
 }
 
 // ---------------------------------------------------------------------------
@@ -62,7 +80,7 @@ __device__ __forceinline__ float2 tof(cd z) { return make_float2((float)z.x, (fl
 // `count` entries starting at table entry offset `first`; L is indexed modulo `lcount`
 // (L shared by every table entry when the symbol has no batch dimension).
 __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int64_t first, int64_t count, double dt,
-                             int integ, int M, double r, float2* __restrict__ tab, int64_t ts) {
+                             int integ, int M, double r, int exact, float2* __restrict__ tab, int64_t ts) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= count) return;
   const int64_t idx = first + k;
@@ -81,21 +99,56 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
     }
     return;
   }
-  // contour sums
+  // phi-function values: s_e1 = (e^z-1)/z, s_e2 = (e^z-1-z)/z^2, s_h = (e^{z/2}-1)/z,
+  // s_a = (-4-z+e^z(4-3z+z^2))/z^3, s_b = (2+z+e^z(z-2))/z^3, s_c = (-4-3z-z^2+e^z(4-z))/z^3
   cd s_e1 = mk(0, 0), s_e2 = mk(0, 0), s_h = mk(0, 0), s_a = mk(0, 0), s_b = mk(0, 0), s_c = mk(0, 0);
-  for (int j = 1; j <= M; ++j) {
-    double sn, cs;
-    sincospi((double)(2 * j - 1) / (double)M, &sn, &cs);
-    const cd z = mk(r * cs, r * sn) + hl;
-    const cd ez = cexpd(z);
-    const cd z2 = z * z, z3 = z2 * z;
-    const cd one = mk(1.0, 0.0);
-    s_e1 = s_e1 + cdiv(ez - one, z);                                       // (e^z - 1)/z
-    s_e2 = s_e2 + cdiv(ez - one - z, z2);                                  // (e^z - 1 - z)/z^2
-    s_h = s_h + cdiv(cexpd(0.5 * z) - one, z);                             // (e^{z/2} - 1)/z
-    s_a = s_a + cdiv(mk(-4.0, 0.0) - z + ez * (mk(4.0, 0.0) - 3.0 * z + z2), z3);  // (-4 - z + e^z(4 - 3z + z^2))/z^3
-    s_b = s_b + cdiv(mk(2.0, 0.0) + z + ez * (mk(-2.0, 0.0) + z), z3);     // (2 + z + e^z(-2 + z))/z^3
-    s_c = s_c + cdiv(mk(-4.0, 0.0) - 3.0 * z - z2 + ez * (mk(4.0, 0.0) - z), z3);  // (-4 - 3z - z^2 + e^z(4 - z))/z^3
+  const cd one = mk(1.0, 0.0);
+  if (exact) {
+    // The mean over M contour points equals the function up to r^M / M! (the host checked that
+    // this is below 1e-10), so the functions are evaluated directly at z = dt L: Taylor series
+    // near 0 (coefficients from expanding e^z), closed forms elsewhere.
+    const cd z = hl;
+    const double az = sqrt(z.x * z.x + z.y * z.y);
+    if (az < 0.5) {
+      cd zk = one;
+      double fact = 1.0;  // k!
+      for (int k = 0; k < 24; ++k) {
+        const double f1 = fact * (k + 1), f2 = f1 * (k + 2), f3 = f2 * (k + 3);  // (k+1)!, (k+2)!, (k+3)!
+        s_e1 = s_e1 + (1.0 / f1) * zk;
+        s_e2 = s_e2 + (1.0 / f2) * zk;
+        s_h = s_h + (ldexp(1.0, -(k + 1)) / f1) * zk;
+        s_a = s_a + ((double)(k + 1) * (k + 1) / f3) * zk;
+        s_b = s_b + ((double)(k + 1) / f3) * zk;
+        s_c = s_c + ((double)(1 - k) / f3) * zk;
+        zk = zk * z;
+        fact = f1;
+      }
+    } else {
+      const cd ez = cexpd(z);
+      const cd z2 = z * z, z3 = z2 * z;
+      s_e1 = cdiv(ez - one, z);
+      s_e2 = cdiv(ez - one - z, z2);
+      s_h = cdiv(cexpd(0.5 * z) - one, z);
+      s_a = cdiv(mk(-4.0, 0.0) - z + ez * (mk(4.0, 0.0) - 3.0 * z + z2), z3);
+      s_b = cdiv(mk(2.0, 0.0) + z + ez * (mk(-2.0, 0.0) + z), z3);
+      s_c = cdiv(mk(-4.0, 0.0) - 3.0 * z - z2 + ez * (mk(4.0, 0.0) - z), z3);
+    }
+    const double m = (double)M;  // the writes below divide by M
+    s_e1 = m * s_e1; s_e2 = m * s_e2; s_h = m * s_h; s_a = m * s_a; s_b = m * s_b; s_c = m * s_c;
+  } else {
+    for (int j = 1; j <= M; ++j) {
+      double sn, cs;
+      sincospi((double)(2 * j - 1) / (double)M, &sn, &cs);
+      const cd z = mk(r * cs, r * sn) + hl;
+      const cd ez = cexpd(z);
+      const cd z2 = z * z, z3 = z2 * z;
+      s_e1 = s_e1 + cdiv(ez - one, z);
+      s_e2 = s_e2 + cdiv(ez - one - z, z2);
+      s_h = s_h + cdiv(cexpd(0.5 * z) - one, z);
+      s_a = s_a + cdiv(mk(-4.0, 0.0) - z + ez * (mk(4.0, 0.0) - 3.0 * z + z2), z3);
+      s_b = s_b + cdiv(mk(2.0, 0.0) + z + ez * (mk(-2.0, 0.0) + z), z3);
+      s_c = s_c + cdiv(mk(-4.0, 0.0) - 3.0 * z - z2 + ez * (mk(4.0, 0.0) - z), z3);
+    }
   }
   const double inv = dt / (double)M;
   auto re = [&](cd s) { return make_float2((float)(inv * s.x), 0.f); };
@@ -166,6 +219,13 @@ int launch_pointwise(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
 }
 
 static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// The M-point contour mean of an entire function around z differs from its value at z by
+// about r^M / M! (the M-th Taylor term); below 1e-10 the tables use the direct evaluation.
+static int phi_exact(const FsmPlan* p) {
+  const double bound = exp((double)p->n_points * log(p->radius) - lgamma((double)p->n_points + 1.0));
+  return bound < 1e-10 ? 1 : 0;
+}
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -354,7 +414,7 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
   const int64_t count = p->tstride;
   const int threads = 128;
   k_phi_tables<<<(unsigned)((count + threads - 1) / threads), threads, 0, st>>>(
-      p->lin, lcount, 0, count, dt, integ, p->n_points, p->radius, p->tab, p->tstride);
+      p->lin, lcount, 0, count, dt, integ, p->n_points, p->radius, phi_exact(p), p->tab, p->tstride);
   if ((rc = cuda_check(cudaGetLastError(), "k_phi_tables"))) {
     free_plan(p);
     return rc;
@@ -374,7 +434,7 @@ int fsm_plan_set_batch_dt(FsmPlan* p, int32_t b, double dt, void* stream) {
   const int64_t lcount = (int64_t)p->lin_src_batch * per;
   const int threads = 128;
   k_phi_tables<<<(unsigned)((per + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
-      p->lin, lcount, (int64_t)b * per, per, dt, p->integ, p->n_points, p->radius, p->tab, p->tstride);
+      p->lin, lcount, (int64_t)b * per, per, dt, p->integ, p->n_points, p->radius, phi_exact(p), p->tab, p->tstride);
   return cuda_check(cudaGetLastError(), "k_phi_tables (batch entry)");
 }
 
@@ -390,6 +450,18 @@ int fsm_plan_move_batch(FsmPlan* p, int32_t dst, int32_t src, void* stream) {
     if (rc) return rc;
   }
   return FSM_OK;
+}
+
+int fsm_plan_tables(const FsmPlan* p, void* dst, size_t capacity_bytes, int32_t* ntab, int64_t* entries,
+                    void* stream) {
+  if (!p) return set_error(FSM_ERR_INVALID, "plan_tables arguments");
+  if (ntab) *ntab = p->ntab;
+  if (entries) *entries = p->tstride;
+  if (!dst) return FSM_OK;
+  const size_t need = (size_t)p->ntab * p->tstride * sizeof(float2);
+  if (capacity_bytes < need) return set_error(FSM_ERR_INVALID, "plan_tables: buffer too small");
+  return cuda_check(cudaMemcpyAsync(dst, p->tab, need, cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                    "copy tables");
 }
 
 int fsm_plan_destroy(FsmPlan* plan) {

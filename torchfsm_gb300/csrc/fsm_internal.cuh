@@ -71,12 +71,22 @@ int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_ks_mean(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_pointwise(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 
+// Raise a kernel's dynamic shared-memory limit when it needs more than 48 KB. The
+// attribute is per function and per device; the size set is remembered per
+// (kernel, device) so that repeated launches skip the driver call.
+bool smem_attr_known(const void* kernel, int device, size_t smem);
+void smem_attr_record(const void* kernel, int device, size_t smem);
+
 template <class K>
 inline int prep_smem(K kernel, size_t smem) {
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute");
-  }
+  if (smem <= 48 * 1024) return FSM_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const void* key = (const void*)kernel;
+  if (smem_attr_known(key, dev, smem)) return FSM_OK;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_check(e, "cudaFuncSetAttribute");
+  smem_attr_record(key, dev, smem);
   return FSM_OK;
 }
 

@@ -208,6 +208,8 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
     if (!a.emit) continue;  // uniform: no further barriers in this group
     __syncthreads();
 
+    // Next-stage fields: each group transforms its own column into tileB, then the CTA
+    // stores the tile with a coalesced mapping (rows of W adjacent columns).
     for (int mf = 0; mf < K::NMG; ++mf) {
       const int f = (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) ? 0 : (mf >> 1);
       const float2* colp = tileA + (f * W + g) * P;
@@ -221,7 +223,7 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
           // 0: psi = -w/lap, 1: i kx psi, 2: w, 3: i kx w
           if (mf < 2) {
             const float lap = -(kxv * kxv + gk.ky * gk.ky);
-            const float il = (lap == 0.f) ? 1.f : 1.f / lap;
+            const float il = (lap == 0.f) ? 1.f : __frcp_rn(lap);
             const float2 psi = cscale(d, -il);
             x = (mf == 0) ? psi : cscale(cmuli(psi), kxv);
           } else {

@@ -428,8 +428,9 @@ def run_serving(args):
     for r in warm:
         serving.solve_alone(r, device, ops)
     total = sum(r.dof_steps for r in reqs)
+    run = server.run_threaded if args.threaded else server.run
     # burst: every request waiting at t = 0
-    wall = server.run(reqs, realtime=False)
+    wall = run(reqs, realtime=False)
     serve_tp = total / wall
     burst_lat = [r.t_done - r.arrival for r in reqs]
     # the plain drop-in, one solve at a time, same requests in the same order
@@ -443,7 +444,7 @@ def run_serving(args):
     # Poisson arrivals at a rate below the server's measured capacity: latency of each request
     rate = args.load * count / wall
     reqs2 = serving.make_stream(count, seed=7, rate_hz=rate)
-    wall2 = server.run(reqs2, realtime=True)
+    wall2 = run(reqs2, realtime=True)
     lat = [r.t_done - r.arrival for r in reqs2]
     ratio = [l / a for l, a in zip(lat, alone_t)]
     line = {"metric": "DOF*steps/s of a mixed solve stream (continuous batching vs one solve at a time)",
@@ -451,6 +452,7 @@ def run_serving(args):
             "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32/c64", "data": "synthetic (seeded band-limited fields)",
             "config": {"workload": f"serving_{count}_requests", "chunk_steps": args.chunk,
+                       "host_loop": "thread per bucket" if args.threaded else "single loop",
                        "mix": "KS 1D L=32pi N in {256..4096} | 2D Burgers nu=0.01 N in {64,128,256}; batch 1-32; "
                               "steps 100-2000; dt 0.01-0.1; ICs |k|<=8, RMS 1 (KS) / 0.25 (Burgers)"},
             "serving": {"throughput_serve": serve_tp, "throughput_plain": plain_tp,
@@ -582,6 +584,7 @@ def main():
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
     ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
+    ap.add_argument("--threaded", type=int, default=1, help="serving: one host worker thread per bucket")
     ap.add_argument("--workload", default="ns2d",
                     choices=["ns2d", "burgers1d", "burgers3d", "serving", "burgers2d_grad"],
                     help="ns2d: the headline (2D NS vorticity 256^2 x 64); burgers1d: 1D Burgers N=128 latency; "

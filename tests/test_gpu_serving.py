@@ -22,6 +22,18 @@ def test_results_same_alone_and_in_the_mix():
         assert torch.isfinite(r.result).all()
 
 
+def test_threaded_loop_gives_the_same_results():
+    device = torch.device("cuda", 0)
+    reqs = serving.make_stream(10, seed=4, rate_hz=0.0, max_steps=120, min_steps=20)
+    server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=13)
+    server.run_threaded(reqs, realtime=False)
+    ops = {}
+    for r in reqs:
+        alone, _ = serving.solve_alone(r, device, ops)
+        err = float((r.result.double() - alone.double()).norm() / alone.double().norm())
+        assert err <= 1e-6 and r.t_done is not None
+
+
 def test_admission_respects_capacity_and_compacts():
     device = torch.device("cuda", 0)
     reqs = [r for r in serving.make_stream(40, seed=5, rate_hz=0.0, max_steps=60, min_steps=10) if r.kind == "ks1d"]

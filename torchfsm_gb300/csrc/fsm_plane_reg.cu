@@ -140,9 +140,19 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
     if (a.stage >= 0) {
       for (int f = 0; f < CG; ++f) {
         const float2* src = a.prod + ((int64_t)b * a.n_prod + cg * CG + f) * S;
-        for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+        // all loads of the tile are issued before the shared-memory stores
+        float2 buf[NX * W / 256];
+#pragma unroll
+        for (int it = 0; it < NX * W / 256; ++it) {
+          const int idx = threadIdx.x + it * 256;
           const int row = idx / W, col = idx % W;
-          if (c0 + col < inner) tileA[(f * W + col) * P + row] = src[(int64_t)row * inner + c0 + col];
+          if (c0 + col < inner) buf[it] = src[(int64_t)row * inner + c0 + col];
+        }
+#pragma unroll
+        for (int it = 0; it < NX * W / 256; ++it) {
+          const int idx = threadIdx.x + it * 256;
+          const int row = idx / W, col = idx % W;
+          if (c0 + col < inner) tileA[(f * W + col) * P + row] = buf[it];
         }
       }
       __syncthreads();
@@ -242,7 +252,9 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
       __syncthreads();
       const int mout = (KIND == FSM_NL_CONVECTION) ? cg * 2 + mf : mf;
       float2* dst = a.mid + ((int64_t)b * a.n_mid + mout) * S;
-      for (int idx = threadIdx.x; idx < NX * W; idx += 256) {
+#pragma unroll
+      for (int it = 0; it < NX * W / 256; ++it) {
+        const int idx = threadIdx.x + it * 256;
         const int row = idx / W, cc = idx % W;
         if (c0 + cc < inner) dst[(int64_t)row * inner + c0 + cc] = tileB[cc * P + row];
       }

@@ -39,9 +39,20 @@ __global__ void __launch_bounds__(256) k_c2c_strided_r(float2* __restrict__ data
   const int64_t c0 = (int64_t)blockIdx.x * W;
   float2* base = data + (int64_t)blockIdx.y * N * inner;
   load_reg_twiddles<N>(twt, master, threadIdx.x, 256);
-  for (int idx = threadIdx.x; idx < N * W; idx += 256) {
-    const int row = idx / W, col = idx % W;
-    if (c0 + col < inner) tile[col * P + row] = base[(int64_t)row * inner + c0 + col];
+  {
+    float2 buf[N * W / 256];
+#pragma unroll
+    for (int it = 0; it < N * W / 256; ++it) {
+      const int idx = threadIdx.x + it * 256;
+      const int row = idx / W, col = idx % W;
+      if (c0 + col < inner) buf[it] = base[(int64_t)row * inner + c0 + col];
+    }
+#pragma unroll
+    for (int it = 0; it < N * W / 256; ++it) {
+      const int idx = threadIdx.x + it * 256;
+      const int row = idx / W, col = idx % W;
+      if (c0 + col < inner) tile[col * P + row] = buf[it];
+    }
   }
   __syncthreads();
   float2 v[E];
@@ -109,11 +120,25 @@ __global__ void __launch_bounds__(256) k_axis1_inv_r(StepArgs a) {
   load_reg_twiddles<NY>(twt, a.tw, threadIdx.x, 256);
   const float2* in0 = a.mid + ((int64_t)b * a.n_mid + 2 * c) * S + (int64_t)x * plane;
   const float2* in1 = in0 + S;
-  for (int idx = threadIdx.x; idx < NY * W; idx += 256) {
-    const int row = idx / W, col = idx % W;
-    if (c0 + col < H) {
-      tA[col * P + row] = in0[(int64_t)row * H + c0 + col];
-      tB[col * P + row] = in1[(int64_t)row * H + c0 + col];
+  {
+    float2 b0[NY * W / 256], b1[NY * W / 256];
+#pragma unroll
+    for (int it = 0; it < NY * W / 256; ++it) {
+      const int idx = threadIdx.x + it * 256;
+      const int row = idx / W, col = idx % W;
+      if (c0 + col < H) {
+        b0[it] = in0[(int64_t)row * H + c0 + col];
+        b1[it] = in1[(int64_t)row * H + c0 + col];
+      }
+    }
+#pragma unroll
+    for (int it = 0; it < NY * W / 256; ++it) {
+      const int idx = threadIdx.x + it * 256;
+      const int row = idx / W, col = idx % W;
+      if (c0 + col < H) {
+        tA[col * P + row] = b0[it];
+        tB[col * P + row] = b1[it];
+      }
     }
   }
   __syncthreads();

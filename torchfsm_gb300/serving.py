@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import collections
 import math
+import threading
 import time
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Tuple
@@ -245,6 +246,71 @@ class SolveServer:
                     busy = True
             if not busy:
                 time.sleep(0.0001)
+        return now()
+
+    def run_threaded(self, requests: List[SolveRequest], realtime: bool = True) -> float:
+        """Serve with one host worker thread per bucket: each worker admits, launches its bucket's
+        ticks and waits for them (the library calls and event waits release the GIL), so host-side
+        launch work of different buckets overlaps. The main thread releases requests at their
+        arrival times. Returns the wall time."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        keys = sorted({(r.kind, r.n) for r in pending})
+        missing = [k for k in keys if k not in self.buckets]
+        if missing:
+            self.prepare(missing)
+        queues = {k: collections.deque() for k in self.buckets}
+        cond = threading.Condition()
+        state = {"arrived": False}
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0
+        device = self.device
+        errors: List[BaseException] = []
+
+        def worker(key):
+            b = self.buckets[key]
+            q = queues[key]
+            try:
+                with torch.cuda.device(device):
+                    while True:
+                        with cond:
+                            while not q and b.n_active == 0 and not state["arrived"]:
+                                cond.wait(0.01)
+                            batch = []
+                            while q and b.capacity - b.n_active - sum(r.batch for r in batch) >= q[0].batch:
+                                batch.append(q.popleft())
+                            finished = state["arrived"] and not q and b.n_active == 0 and not batch
+                        if finished:
+                            return
+                        for r in batch:
+                            b.admit(r, now())
+                        if b.n_active == 0:
+                            continue
+                        b.launch()
+                        b.tick[1].synchronize()
+                        for r in b.poll():
+                            r._copied.synchronize()
+                            r.t_done = now()
+            except BaseException as e:  # surface worker failures to the caller
+                errors.append(e)
+
+        threads = [threading.Thread(target=worker, args=(k,), daemon=True) for k in self.buckets]
+        for th in threads:
+            th.start()
+        for r in pending:
+            if realtime:
+                delay = r.arrival - now()
+                if delay > 0:
+                    time.sleep(delay)
+            with cond:
+                queues[(r.kind, r.n)].append(r)
+                cond.notify_all()
+        with cond:
+            state["arrived"] = True
+            cond.notify_all()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
         return now()
 
     @property

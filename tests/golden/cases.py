@@ -127,6 +127,13 @@ CASES = {
         lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")],
         ic=_bl(71, (32, 32), 4, 0.5),
     ),
+    # 1D KSConvection with the mean removed over a batch of three samples.
+    "ksnd1d_b3_n64": dict(
+        mesh=[(0, 10 * math.pi, 64)], batch=3, channels=1, dt=0.05, step=40, record=8,
+        build=lambda M: M.pde.KuramotoSivashinskyHighDim(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")],
+        ic=_bl(113, (64,), 6, 0.7),
+    ),
     # Velocity-form NS with the Leray projection.
     "nsvel2d_n32": dict(
         mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=1, channels=2, dt=0.01, step=20, record=0,

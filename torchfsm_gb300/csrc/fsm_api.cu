@@ -473,7 +473,11 @@ int fsm_plan_destroy(FsmPlan* plan) {
 
 static size_t workspace_layout(const FsmPlan* p, int32_t batch, int32_t steps, size_t* off_arrays) {
   size_t bytes = align256((size_t)(steps + 1) * sizeof(int32_t));  // record slots
-  bytes += 256;                                                    // KS batch-mean scratch
+  size_t dc = 256;                                                 // KS batch-mean scratch
+  if (p->path == 1 && p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN))
+    // 1D: per-stage k = 0 products, initial k = 0 values, per-stage batch means
+    dc = align256(((size_t)steps * p->nstages * (batch + 1) + batch) * sizeof(float2));
+  bytes += dc;
   if (off_arrays) *off_arrays = bytes;
   if (p->path == 2 || p->path == 4) {
     const size_t per = (size_t)(p->n_aux * p->C + p->n_mid + p->n_mid2 + p->n_prod) * p->S * sizeof(float2);
@@ -494,6 +498,8 @@ int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches)
     const int64_t per_stage = (plan->path == 4 ? 4 : 2) +
                               ((plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) ? 1 : 0);
     *launches = 1 + (int64_t)steps * plan->nstages * per_stage;
+  } else if (plan->path == 1 && plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) {
+    *launches = steps > 0 ? 3 : 1;  // line kernel, batch means of k = 0, k = 0 fix-up
   } else {
     *launches = 1;
   }
@@ -581,8 +587,6 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
     }
   }
   if (any_record && !traj) return set_error(FSM_ERR_INVALID, "trajectory buffer missing");
-  if (p->path == 1 && p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN) && batch > 1)
-    return set_error(FSM_ERR_UNSUPPORTED, "1D KS mean removal over a batch > 1");
 
   char* ws = (char*)workspace;
   int32_t* d_slots = (int32_t*)ws;
@@ -613,7 +617,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
   a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
-  a.dc = (float2*)(ws + off_arrays - 256);
+  a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));
   a.coef = p->nl_coef;
   a.scale = (float)(1.0 / (double)p->R);
   a.C = p->C;

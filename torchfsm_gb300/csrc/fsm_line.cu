@@ -63,6 +63,8 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
   const float2* tab = a.tab + toff;
   const float2* src = a.src ? a.src + (int64_t)(a.src_batch > 1 ? b : 0) * H : nullptr;
   const int slot0 = a.slots ? a.slots[0] : -1;
+  if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && t == 0)
+    a.dc[(int64_t)a.steps * a.nstages * a.B + b] = u[0];  // initial k = 0 value
   for (int k = t; k < H; k += G) {
     if (slot0 >= 0) a.traj[((int64_t)b * a.n_frames + slot0) * H + k] = u[k];
     if (a.steps > 0) line_build<N, KIND>(Z, k, u[k], (float)a.keepx[k], a.kx[k], a.scale);
@@ -84,7 +86,9 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
       const int slot = (last && a.slots) ? a.slots[step + 1] : -1;
       for (int k = t; k < H; k += G) {
         float2 nv = cscale(Z[k], a.coef);
-        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && k == 0) nv = make_float2(0.f, 0.f);
+        // k = 0 of the product, for the batch-mean fix-up (k_line_dc_fixup)
+        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && k == 0)
+          a.dc[((int64_t)step * ns + s) * a.B + b] = Z[0];
         if (src) nv = cadd(nv, src[k]);
         const float2 nxt = etd_stage(a.integ, s, nv, u + k, acc + k, q + k, tab + k, a.ts);
         if (!final_stage) line_build<N, KIND>(Z, k, nxt, (float)a.keepx[k], a.kx[k], a.scale);
@@ -121,10 +125,66 @@ static int launch_line_kind(int n, const StepArgs& a, cudaStream_t st) {
   return set_error(FSM_ERR_UNSUPPORTED, "1D: unsupported length " + std::to_string(n));
 }
 
+// KSConvection with the mean removed over a batch (operator/dedicated/_ks_convection.py:35-36:
+// re.mean() spans the whole batch). The mean only changes the k = 0 value of the nonlinear
+// term, and the k = 0 mode never feeds back into the product (it is a gradient), so the line
+// kernel runs with the per-sample values and records every stage's k = 0 product P_b in
+// dc[step][stage][b]. k_line_dc_mean reduces each (step, stage) row over the batch, in a fixed
+// order, into dc[steps * stages * B + B + row]; k_line_dc_fixup then replays the k = 0
+// recurrence of each sample with coef * (P_b - mean) + source, the same arithmetic as the line
+// kernel, and overwrites k = 0 of the state and of the recorded frames.
+__global__ void __launch_bounds__(256) k_line_dc_mean(StepArgs a) {
+  __shared__ float2 red[256];
+  const int row = blockIdx.x;
+  const float2* P = a.dc + (int64_t)row * a.B;
+  float2 sum = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < a.B; i += 256) sum = cadd(sum, P[i]);
+  red[threadIdx.x] = sum;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float inv = 1.f / (float)a.B;
+    a.dc[(int64_t)a.steps * a.nstages * a.B + a.B + row] = cscale(red[0], inv);
+  }
+}
+
+__global__ void k_line_dc_fixup(StepArgs a) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.B) return;
+  const int ns = a.nstages;
+  const int H = a.H;
+  const float2* mean = a.dc + (int64_t)a.steps * ns * a.B + a.B;
+  float2 u = a.dc[(int64_t)a.steps * ns * a.B + b];
+  float2 acc = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
+  const float2* tab = a.tab + (int64_t)(a.lin_batch > 1 ? b : 0) * H;
+  const float2 src0 = a.src ? a.src[(int64_t)(a.src_batch > 1 ? b : 0) * H] : make_float2(0.f, 0.f);
+  for (int step = 0; step < a.steps; ++step) {
+    for (int s = 0; s < ns; ++s) {
+      const int64_t row = (int64_t)step * ns + s;
+      const float2 nv = cadd(cscale(csub(a.dc[row * a.B + b], mean[row]), a.coef), src0);
+      (void)etd_stage(a.integ, s, nv, &u, &acc, &q, tab, a.ts);
+    }
+    const int slot = a.slots ? a.slots[step + 1] : -1;
+    if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H] = u;
+  }
+  a.state[(int64_t)b * H] = u;
+}
+
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {
   switch (p->nl) {
     case FSM_NL_CONVECTION: return launch_line_kind<FSM_NL_CONVECTION>(p->n[0], a, st);
-    case FSM_NL_KS: return launch_line_kind<FSM_NL_KS>(p->n[0], a, st);
+    case FSM_NL_KS: {
+      int rc = launch_line_kind<FSM_NL_KS>(p->n[0], a, st);
+      if (rc || !(p->flags & FSM_FLAG_REMOVE_MEAN) || a.steps == 0) return rc;
+      k_line_dc_mean<<<a.steps * a.nstages, 256, 0, st>>>(a);
+      rc = cuda_check(cudaGetLastError(), "k_line_dc_mean");
+      if (rc) return rc;
+      k_line_dc_fixup<<<(a.B + 127) / 128, 128, 0, st>>>(a);
+      return cuda_check(cudaGetLastError(), "k_line_dc_fixup");
+    }
   }
   return set_error(FSM_ERR_UNSUPPORTED, "1D: unsupported nonlinear term");
 }

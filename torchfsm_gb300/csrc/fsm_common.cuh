@@ -72,76 +72,95 @@ __host__ __device__ inline int scheme_aux(int integ) {
 //           a2 = q + 2 c2 n1, u' = acc + c5 n2.
 //  (S)ETDRK2: a1 = E u + c1 n0, acc = a1 - c2 n0, u' = acc + c2 n1.
 //  (S)ETDRK1: u' = E u + c1 n0.
+template <int INTEG, int S>
+__device__ __forceinline__ float2 etd_stage_c(float2 nv, float2* __restrict__ u, float2* __restrict__ acc,
+                                              float2* __restrict__ q, const float2* __restrict__ tab, int64_t ts) {
+  if (INTEG == FSM_SETDRK4) {
+    if (S == 0) {
+      const float2 uu = *u;
+      const float2 E = tab[0], E2 = tab[ts], c1 = tab[2 * ts], c4 = tab[3 * ts];
+      const float2 a1 = cfma(c1, nv, cmul(E2, uu));
+      *acc = cfma(c4, nv, cmul(E, uu));
+      *q = cfma(make_float2(-c1.x, -c1.y), nv, cmul(E2, a1));
+      return a1;
+    } else if (S == 1) {
+      const float2 uu = *u;
+      const float2 E2 = tab[ts], c1 = tab[2 * ts], c5 = tab[4 * ts];
+      *acc = cfma(cscale(c5, 2.f), nv, *acc);
+      return cfma(c1, nv, cmul(E2, uu));
+    } else if (S == 2) {
+      const float2 c1 = tab[2 * ts], c5 = tab[4 * ts];
+      *acc = cfma(cscale(c5, 2.f), nv, *acc);
+      return cfma(cscale(c1, 2.f), nv, *q);
+    } else {
+      const float2 c6 = tab[5 * ts];
+      const float2 un = cfma(c6, nv, *acc);
+      *u = un;
+      return un;
+    }
+  } else if (INTEG == FSM_SETDRK3) {
+    if (S == 0) {
+      const float2 uu = *u;
+      const float2 E = tab[0], E2 = tab[ts], c1 = tab[2 * ts], c2 = tab[3 * ts], c3 = tab[4 * ts];
+      const float2 Eu = cmul(E, uu);
+      *acc = cfma(c3, nv, Eu);
+      *q = cfma(make_float2(-c2.x, -c2.y), nv, Eu);
+      return cfma(c1, nv, cmul(E2, uu));
+    } else if (S == 1) {
+      const float2 c2 = tab[3 * ts], c4 = tab[5 * ts];
+      *acc = cfma(c4, nv, *acc);
+      return cfma(cscale(c2, 2.f), nv, *q);
+    } else {
+      const float2 c5 = tab[6 * ts];
+      const float2 un = cfma(c5, nv, *acc);
+      *u = un;
+      return un;
+    }
+  } else if (INTEG == FSM_SETDRK2 || INTEG == FSM_ETDRK2) {
+    if (S == 0) {
+      const float2 uu = *u;
+      const float2 E = tab[0], c1 = tab[ts], c2 = tab[2 * ts];
+      const float2 a1 = cfma(c1, nv, cmul(E, uu));
+      *acc = cfma(make_float2(-c2.x, -c2.y), nv, a1);
+      return a1;
+    } else {
+      const float2 c2 = tab[2 * ts];
+      const float2 un = cfma(c2, nv, *acc);
+      *u = un;
+      return un;
+    }
+  } else {  // (S)ETDRK1, ETDRK0
+    const float2 E = tab[0], c1 = tab[ts];
+    const float2 un = cfma(c1, nv, cmul(E, *u));
+    *u = un;
+    return un;
+  }
+}
+
+// Run-time dispatch onto etd_stage_c.
 __device__ __forceinline__ float2 etd_stage(int integ, int s, float2 nv, float2* __restrict__ u,
                                             float2* __restrict__ acc, float2* __restrict__ q,
                                             const float2* __restrict__ tab, int64_t ts) {
   switch (integ) {
-    case FSM_SETDRK4: {
-      if (s == 0) {
-        const float2 uu = *u;
-        const float2 E = tab[0], E2 = tab[ts], c1 = tab[2 * ts], c4 = tab[3 * ts];
-        const float2 a1 = cfma(c1, nv, cmul(E2, uu));
-        *acc = cfma(c4, nv, cmul(E, uu));
-        *q = cfma(make_float2(-c1.x, -c1.y), nv, cmul(E2, a1));
-        return a1;
-      } else if (s == 1) {
-        const float2 uu = *u;
-        const float2 E2 = tab[ts], c1 = tab[2 * ts], c5 = tab[4 * ts];
-        *acc = cfma(cscale(c5, 2.f), nv, *acc);
-        return cfma(c1, nv, cmul(E2, uu));
-      } else if (s == 2) {
-        const float2 c1 = tab[2 * ts], c5 = tab[4 * ts];
-        *acc = cfma(cscale(c5, 2.f), nv, *acc);
-        return cfma(cscale(c1, 2.f), nv, *q);
-      } else {
-        const float2 c6 = tab[5 * ts];
-        const float2 un = cfma(c6, nv, *acc);
-        *u = un;
-        return un;
+    case FSM_SETDRK4:
+      switch (s) {
+        case 0: return etd_stage_c<FSM_SETDRK4, 0>(nv, u, acc, q, tab, ts);
+        case 1: return etd_stage_c<FSM_SETDRK4, 1>(nv, u, acc, q, tab, ts);
+        case 2: return etd_stage_c<FSM_SETDRK4, 2>(nv, u, acc, q, tab, ts);
+        default: return etd_stage_c<FSM_SETDRK4, 3>(nv, u, acc, q, tab, ts);
       }
-    }
-    case FSM_SETDRK3: {
-      if (s == 0) {
-        const float2 uu = *u;
-        const float2 E = tab[0], E2 = tab[ts], c1 = tab[2 * ts], c2 = tab[3 * ts], c3 = tab[4 * ts];
-        const float2 Eu = cmul(E, uu);
-        *acc = cfma(c3, nv, Eu);
-        *q = cfma(make_float2(-c2.x, -c2.y), nv, Eu);
-        return cfma(c1, nv, cmul(E2, uu));
-      } else if (s == 1) {
-        const float2 c2 = tab[3 * ts], c4 = tab[5 * ts];
-        *acc = cfma(c4, nv, *acc);
-        return cfma(cscale(c2, 2.f), nv, *q);
-      } else {
-        const float2 c5 = tab[6 * ts];
-        const float2 un = cfma(c5, nv, *acc);
-        *u = un;
-        return un;
+    case FSM_SETDRK3:
+      switch (s) {
+        case 0: return etd_stage_c<FSM_SETDRK3, 0>(nv, u, acc, q, tab, ts);
+        case 1: return etd_stage_c<FSM_SETDRK3, 1>(nv, u, acc, q, tab, ts);
+        default: return etd_stage_c<FSM_SETDRK3, 2>(nv, u, acc, q, tab, ts);
       }
-    }
     case FSM_SETDRK2:
-    case FSM_ETDRK2: {
-      if (s == 0) {
-        const float2 uu = *u;
-        const float2 E = tab[0], c1 = tab[ts], c2 = tab[2 * ts];
-        const float2 a1 = cfma(c1, nv, cmul(E, uu));
-        *acc = cfma(make_float2(-c2.x, -c2.y), nv, a1);
-        return a1;
-      } else {
-        const float2 c2 = tab[2 * ts];
-        const float2 un = cfma(c2, nv, *acc);
-        *u = un;
-        return un;
-      }
-    }
-    case FSM_SETDRK1:
-    case FSM_ETDRK1:
-    default: {
-      const float2 E = tab[0], c1 = tab[ts];
-      const float2 un = cfma(c1, nv, cmul(E, *u));
-      *u = un;
-      return un;
-    }
+    case FSM_ETDRK2:
+      return s == 0 ? etd_stage_c<FSM_SETDRK2, 0>(nv, u, acc, q, tab, ts)
+                    : etd_stage_c<FSM_SETDRK2, 1>(nv, u, acc, q, tab, ts);
+    default:
+      return etd_stage_c<FSM_SETDRK1, 0>(nv, u, acc, q, tab, ts);
   }
 }
 

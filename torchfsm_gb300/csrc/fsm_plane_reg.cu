@@ -108,6 +108,69 @@ __device__ __forceinline__ void nv_leray(float2 (&nv)[CG], const PointK<DIM>& pk
   for (int c = 0; c < CG; ++c) nv[c] = out[c];
 }
 
+// Phase 2 of k_axis0_r: the stage update at every point of the tile, in a coalesced point
+// mapping, leaving the masked next-stage field in tileA. INTEG/STG name the scheme and stage
+// at compile time (so that the loads of several points are issued together); -1 dispatches
+// at run time.
+template <int NX, int KIND, int DIM, int INTEG, int STG>
+__device__ __forceinline__ void axis0_update(const StepArgs& a, float2* __restrict__ tileA, int b, int64_t c0, int cg,
+                                             bool last) {
+  using Cfg = ColCfg<NX>;
+  using K = RegKind<KIND, DIM>;
+  constexpr int W = Cfg::W, P = Cfg::P, C = K::C, CG = K::CG;
+  const int64_t S = a.S;
+  const int64_t inner = S / NX;
+  const bool update = STG >= 0 || a.stage >= 0;  // false: the priming launch (mask and emit only)
+  // restrict-qualified views so that loads of later points may be issued ahead of the stores of earlier ones
+  float2* __restrict__ state = a.state;
+  float2* __restrict__ aux = a.aux;
+  float2* __restrict__ traj = a.traj;
+  const float2* __restrict__ tab = a.tab;
+  const float2* __restrict__ srcp = a.src;
+  constexpr int PPT = NX * W / 256;  // points per thread
+#pragma unroll 4
+  for (int it = 0; it < PPT; ++it) {
+    const int idx = threadIdx.x + it * 256;
+    const int row = idx / W, col = idx % W;
+    const int64_t j = c0 + col;
+    if (j >= inner) continue;
+    const int64_t sidx = (int64_t)row * inner + j;
+    const PointK<DIM> pk = point_k<DIM>(a, row, j);
+    float2 nv[CG];
+    if (update) {
+#pragma unroll
+      for (int f = 0; f < CG; ++f) nv[f] = tileA[(f * W + col) * P + row];
+      if (KIND == FSM_NL_LERAY) nv_leray<DIM, CG>(nv, pk, row, j, a, NX);
+      if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv[0] = csub(nv[0], a.dc[0]);
+#pragma unroll
+      for (int f = 0; f < CG; ++f) {
+        const int c = cg * CG + f;
+        nv[f] = cscale(nv[f], a.coef);
+        if (srcp) nv[f] = cadd(nv[f], srcp[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < CG; ++f) {
+      const int c = cg * CG + f;
+      float2* up = state + ((int64_t)b * C + c) * S + sidx;
+      float2 st;
+      if (!update) {
+        st = *up;
+      } else {
+        float2* accp = aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
+        float2* qp = aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
+        const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+        if (STG >= 0)
+          st = etd_stage_c<INTEG, STG>(nv[f], up, accp, qp, tab + toff, a.ts);
+        else
+          st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, tab + toff, a.ts);
+      }
+      if (a.slot >= 0 && (!update || last)) traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
+      tileA[(f * W + col) * P + row] = cscale(st, pk.mask);
+    }
+  }
+}
+
 // Axis-0 pass (2D: the column pass; 3D: the x pass). A CTA owns W adjacent
 // inner columns (contiguous in memory) of one sample, all NX rows:
 //   1. forward transform along axis 0 of the products -> N (+ Leray projection, + source)
@@ -168,52 +231,15 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
     }
     __syncthreads();
 
-    {
-      // restrict-qualified views so that loads of later points may be issued ahead of the stores of earlier ones
-      float2* __restrict__ state = a.state;
-      float2* __restrict__ aux = a.aux;
-      float2* __restrict__ traj = a.traj;
-      const float2* __restrict__ tab = a.tab;
-      const float2* __restrict__ srcp = a.src;
-      constexpr int PPT = NX * W / 256;  // points per thread
-#pragma unroll 4
-      for (int it = 0; it < PPT; ++it) {
-        const int idx = threadIdx.x + it * 256;
-        const int row = idx / W, col = idx % W;
-        const int64_t j = c0 + col;
-        if (j >= inner) continue;
-        const int64_t sidx = (int64_t)row * inner + j;
-        const PointK<DIM> pk = point_k<DIM>(a, row, j);
-        float2 nv[CG];
-        if (a.stage >= 0) {
-#pragma unroll
-          for (int f = 0; f < CG; ++f) nv[f] = tileA[(f * W + col) * P + row];
-          if (KIND == FSM_NL_LERAY) nv_leray<DIM, CG>(nv, pk, row, j, a, NX);
-          if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv[0] = csub(nv[0], a.dc[0]);
-#pragma unroll
-          for (int f = 0; f < CG; ++f) {
-            const int c = cg * CG + f;
-            nv[f] = cscale(nv[f], a.coef);
-            if (srcp) nv[f] = cadd(nv[f], srcp[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + sidx]);
-          }
-        }
-#pragma unroll
-        for (int f = 0; f < CG; ++f) {
-          const int c = cg * CG + f;
-          float2* up = state + ((int64_t)b * C + c) * S + sidx;
-          float2 st;
-          if (a.stage < 0) {
-            st = *up;
-          } else {
-            float2* accp = aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
-            float2* qp = aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
-            const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
-            st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, tab + toff, a.ts);
-          }
-          if (a.slot >= 0 && (a.stage < 0 || last)) traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
-          tileA[(f * W + col) * P + row] = cscale(st, pk.mask);
-        }
+    if (a.stage >= 0 && a.integ == FSM_SETDRK4) {
+      switch (a.stage) {
+        case 0: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 0>(a, tileA, b, c0, cg, last); break;
+        case 1: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 1>(a, tileA, b, c0, cg, last); break;
+        case 2: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 2>(a, tileA, b, c0, cg, last); break;
+        default: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 3>(a, tileA, b, c0, cg, last); break;
       }
+    } else {
+      axis0_update<NX, KIND, DIM, -1, -1>(a, tileA, b, c0, cg, last);
     }
     if (!a.emit) continue;  // uniform: no further barriers in this group
     __syncthreads();

@@ -228,9 +228,71 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
 
     # instrumented pass: per-kernel CUDA-event timing of one integration
     prof = profile_kernels(plan, state0, ws, device)
+
+    # the reference's torch GPU path on the same inputs (rank 0 only)
+    torch_ref = None
+    if rank == 0 and not args.no_torch_reference:
+        def ours_after(k):
+            return op.integrate(u_0=u_dev, dt=DT, step=k)
+
+        torch_ref = torch_gpu_reference(device, w0, ours_half=ours_after)
     return {"ms": ms, "e2e_ms": e2e_ms, "finite": finite, "clocks": clk.summary(), "launches": launches_per_step,
             "prof": prof, "h2d": host_in.numel() * 4, "d2h": out_h.numel() * out_h.element_size(),
-            "B": B}
+            "B": B, "torch_ref": torch_ref}
+
+
+def torch_gpu_reference(device, w0: np.ndarray, ours_half=None, k1: int = 10, k2: int = 60) -> dict:
+    """The reference's own torch path (cuFFT + ATen) on the same GPU, same config and inputs.
+
+    Runs the unmodified reference package installed under baseline/_ref through its public
+    API (NavierStokesVorticity(1000).integrate on a cuda MeshGrid, default SETDRK4). Each
+    integrate call carries a fixed host cost (gc.collect + empty_cache), so the steady
+    per-step time is the difference of a k2-step and a k1-step call, both timed with CUDA
+    events. Where our final state after k1 steps is given, the rel-L2 distance of the two
+    FP32 results is reported as well."""
+    import torch
+
+    ref = os.path.join(REPO, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "torchfsm")):
+        return {"unavailable": "reference not installed under baseline/_ref"}
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    try:
+        import torchfsm as R
+        from torchfsm.mesh import MeshGrid
+        from torchfsm.pde import NavierStokesVorticity
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference import failed: {type(e).__name__}: {e}"}
+    mesh = MeshGrid(MESH, device=device)
+    op = NavierStokesVorticity(RE)
+    u = torch.tensor(w0, device=device)
+    u = u if u.dim() == 4 else u.unsqueeze(1)
+    op.integrate(u_0=u, mesh=mesh, dt=DT, step=2)  # registers the mesh, builds the coefficients
+    torch.cuda.synchronize()
+
+    def timed(k):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record()
+        out = op.integrate(u_0=u, dt=DT, step=k)
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1), (time.perf_counter() - t0) * 1e3, out
+
+    t1, w1, out1 = timed(k1)
+    t2, w2, _ = timed(k2)
+    per_step = (t2 - t1) / (k2 - k1)
+    B = u.shape[0]
+    res = {"value": B * N * N / (per_step * 1e-3), "unit": "DOF*steps/s", "ms_per_step": per_step,
+           "steps_timed": [k1, k2], "call_ms": [t1, t2], "kind": "reference torch path (cuFFT + ATen), FP32",
+           "version": getattr(R, "__version__", "0.0.4")}
+    if ours_half is not None:
+        ours = ours_half(k1)
+        res["rel_l2_vs_fused_after_%d_steps" % k1] = float(
+            torch.linalg.vector_norm(ours - out1) / torch.linalg.vector_norm(out1))
+    return res
 
 
 def profile_kernels(plan, state0, ws, device) -> dict:
@@ -581,6 +643,8 @@ def main():
     ap.add_argument("--impl", default="fused", choices=["fused", "reference"])
     ap.add_argument("--cpu-samples", type=int, default=16)
     ap.add_argument("--cpu-time-steps", type=int, default=5)
+    ap.add_argument("--no-torch-reference", action="store_true",
+                    help="skip the reference torch GPU path leg of the ns2d workload")
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
     ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
@@ -663,7 +727,7 @@ def main():
         "e2e": {"value": e2e_value, "unit": "DOF*steps/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"], "ms_per_step": res["e2e_ms"]},
         "gpu_launches": res["launches"] * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_plane_col (column pass)",
+        "roofline": {"bound": "hbm", "kernel": "k_axis0_r<256, VORTICITY, 2> (column pass)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": None,
                      "peak_source": f"{peak_kind} hbm_gbs",
@@ -671,8 +735,13 @@ def main():
                      "step_model_bytes_per_dof_step": 212,
                      "step_achieved_gbs": 212.0 * dof_steps / world / (res["ms"] * 1e-3) / 1e9 * world},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "torch_gpu_reference": res["torch_ref"],
         "clocks": res["clocks"],
     }
+    tr = res["torch_ref"]
+    if tr and "value" in tr:
+        tr["fused_device_over_reference"] = value / tr["value"]
+        tr["fused_e2e_over_reference"] = e2e_value / tr["value"]
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

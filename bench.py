@@ -317,6 +317,11 @@ def profile_kernels(plan, state0, ws, device) -> dict:
             for i in range(4)}
 
 
+# DRAM bytes of one column-pass launch at batch 64, from one ncu capture of `bench.py --ncu-case`
+# (dram__bytes_read.sum 35.1 MB + dram__bytes_write.sum 42.3 MB, stage 0 of a SETDRK4 step).
+COLUMN_PASS_DRAM_BYTES = 77.3e6
+
+
 def column_pass_bytes(B: int) -> float:
     """Algorithmic bytes of one column-pass launch, averaged over the four SETDRK4 stages.
 
@@ -729,7 +734,9 @@ def main():
         "gpu_launches": res["launches"] * args.steps,
         "roofline": {"bound": "hbm", "kernel": "k_axis0_r<256, VORTICITY, 2> (column pass)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None, "traffic": COLUMN_PASS_DRAM_BYTES,
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one stage-0 column pass "
+                                     "launch of this workload (bench.py --ncu-case)",
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "per_kernel_ms": {k: v["avg_ms"] for k, v in res["prof"].items() if v["launches"]},
                      "step_model_bytes_per_dof_step": 212,

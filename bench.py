@@ -508,18 +508,27 @@ def run_serving(args):
         ref = res.double()
         max_err = max(max_err, float((r.result.double() - ref).norm() / max(ref.norm(), 1e-30)))
     plain_tp = total / sum(alone_t)
-    # Poisson arrivals at a rate below the server's measured capacity: latency of each request
-    rate = args.load * count / wall
-    reqs2 = serving.make_stream(count, seed=7, rate_hz=rate)
-    wall2 = run(reqs2, realtime=True)
-    lat = [r.t_done - r.arrival for r in reqs2]
-    ratio = [l / a for l, a in zip(lat, alone_t)]
+    # Poisson arrivals at rates below the server's measured capacity: latency of each request
+    # against its own one-at-a-time time (the streams hold the same requests at every rate)
+    sweep = []
+    for load in sorted({args.load, 0.35}):
+        rq = serving.make_stream(count, seed=7, rate_hz=load * count / wall)
+        w = run(rq, realtime=True)
+        lt = [r.t_done - r.arrival for r in rq]
+        rt = [l / a for l, a in zip(lt, alone_t)]
+        sweep.append({"load": load, "rate_hz": load * count / wall, "wall_s": w,
+                      "latency_s": {"p50": _pctl(lt, 50), "p99": _pctl(lt, 99)},
+                      "latency_over_isolated": {"p50": _pctl(rt, 50), "p99": _pctl(rt, 99)},
+                      "p99_over_isolated_p99": _pctl(lt, 99) / _pctl(alone_t, 99)})
+        if load == args.load:
+            rate, wall2, lat, ratio = load * count / wall, w, lt, rt
     line = {"metric": "DOF*steps/s of a mixed solve stream (continuous batching vs one solve at a time)",
             "value": serve_tp, "unit": "DOF*steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32/c64", "data": "synthetic (seeded band-limited fields)",
             "config": {"workload": f"serving_{count}_requests", "chunk_steps": args.chunk,
                        "host_loop": "thread per bucket" if args.threaded else "single loop",
+                       "cuda_graphs": f"replayed per (slots, steps) shape for ticks of <= {serving.GRAPH_MAX_STEPS} steps",
                        "mix": "KS 1D L=32pi N in {256..4096} | 2D Burgers nu=0.01 N in {64,128,256}; batch 1-32; "
                               "steps 100-2000; dt 0.01-0.1; ICs |k|<=8, RMS 1 (KS) / 0.25 (Burgers)"},
             "serving": {"throughput_serve": serve_tp, "throughput_plain": plain_tp,
@@ -529,6 +538,7 @@ def run_serving(args):
                         "latency_s": {"p50": _pctl(lat, 50), "p99": _pctl(lat, 99)},
                         "isolated_latency_s": {"p50": _pctl(alone_t, 50), "p99": _pctl(alone_t, 99)},
                         "latency_over_isolated": {"p50": _pctl(ratio, 50), "p99": _pctl(ratio, 99)},
+                        "poisson_sweep": sweep, "graph_replays": server.graph_replays,
                         "max_rel_diff_mix_vs_alone": max_err},
             "gpu_launches": server.launches,
             "e2e": {"value": serve_tp, "unit": "DOF*steps/s",

@@ -42,3 +42,19 @@ def test_admission_respects_capacity_and_compacts():
     for b in server.buckets.values():
         assert b.n_active == 0 and all(o is None for o in b.owner)
     assert all(r.result is not None and r.t_done >= r.t_admit for r in reqs)
+
+
+def test_graph_replays_match_direct_launches():
+    device = torch.device("cuda", 0)
+    out = {}
+    for graphs in (False, True):
+        reqs = serving.make_stream(12, seed=6, rate_hz=0.0, max_steps=90, min_steps=30)
+        server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=8, graphs=graphs)
+        server.run(reqs, realtime=False)
+        out[graphs] = [r.result for r in reqs]
+        if graphs:
+            assert server.graph_replays > 0
+        else:
+            assert server.graph_replays == 0
+    for a, b in zip(out[False], out[True]):
+        assert torch.equal(a, b)

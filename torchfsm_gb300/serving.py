@@ -80,11 +80,21 @@ def slot_bytes(kind: str, n: int, chunk: int) -> int:
     return per_field * (C + 2 * C + 4 + C + 6)
 
 
+# Ticks of at most GRAPH_MAX_STEPS steps replay a CUDA graph captured per (active slots, steps);
+# the step count of such ticks is rounded down to a power of two so that few shapes recur.
+GRAPH_MAX_STEPS = 64
+GRAPH_CACHE = 48
+
+
 class _Bucket:
     def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int,
-                 priority: int = 0, tick_ms: float = 4.0):
+                 priority: int = 0, tick_ms: float = 4.0, graphs: bool = True):
         self.kind, self.n, self.capacity, self.device, self.chunk = kind, n, capacity, device, chunk
         self.tick_ms = tick_ms
+        self.use_graphs = graphs
+        self.graphs: "collections.OrderedDict[Tuple[int, int], torch.cuda.CUDAGraph]" = collections.OrderedDict()
+        self._seen: set = set()
+        self.replays = 0
         self.step_ms: Optional[float] = None  # measured device time per step and slot
         op, mesh, C = problem(kind, n)
         self.C = C
@@ -128,14 +138,45 @@ class _Bucket:
         if self.step_ms:
             # ticks of about tick_ms of device work keep admission and small requests responsive
             k = max(1, min(k, int(self.tick_ms / (self.step_ms * self.n_active))))
+        if self.use_graphs and k <= GRAPH_MAX_STEPS:
+            k = 1 << (k.bit_length() - 1)
         with torch.cuda.stream(self.stream):
             e0 = torch.cuda.Event(enable_timing=True)
             e0.record(self.stream)
-            self.plan.integrate_half(self.state[: self.n_active], k, workspace=self.ws)
+            self._advance(self.n_active, k)
             e1 = torch.cuda.Event(enable_timing=True)
             e1.record(self.stream)
         self.launches += self.plan.launch_count(k)
         self.tick = (e0, e1, k, self.n_active)
+
+    def _advance(self, n: int, k: int) -> None:
+        """k steps of slots [0, n) on the bucket's stream (the current stream here): a replay of the
+        graph of (n, k) when there is one. A shape is captured the second time it occurs (the first
+        run sets the kernels' attributes); the capture is thread-local, so the other buckets' host
+        threads keep launching meanwhile."""
+        if not self.use_graphs or k > GRAPH_MAX_STEPS:
+            self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
+            return
+        key = (n, k)
+        g = self.graphs.get(key)
+        if g is None:
+            if key not in self._seen:
+                self._seen.add(key)
+                self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
+                return
+            g = torch.cuda.CUDAGraph()
+            g.capture_begin(capture_error_mode="thread_local")
+            try:
+                self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
+            finally:
+                g.capture_end()
+            self.graphs[key] = g
+            while len(self.graphs) > GRAPH_CACHE:
+                self.graphs.popitem(last=False)
+        else:
+            self.graphs.move_to_end(key)
+        g.replay()
+        self.replays += 1
 
     def poll(self) -> List[SolveRequest]:
         """Finish the tick if the device is done with it; return the requests that completed, whose
@@ -189,8 +230,9 @@ class SolveServer:
     """Admission by HBM budget, per-bucket ticks on separate streams."""
 
     def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
-                 max_slots: int = 256, tick_ms: float = 4.0):
+                 max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True):
         self.device = device
+        self.graphs = graphs
         self.budget = hbm_budget_bytes
         self.chunk = chunk
         self.max_slots = max_slots
@@ -205,7 +247,7 @@ class SolveServer:
             cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
             # cheap per-step buckets (1D, small 2D grids) get the higher-priority streams
             prio = hi if (kind == "ks1d" or n <= 64) else lo
-            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms)
+            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms, self.graphs)
         torch.cuda.synchronize(self.device)
 
     def run(self, requests: List[SolveRequest], realtime: bool = True) -> float:
@@ -317,6 +359,10 @@ class SolveServer:
     def launches(self) -> int:
         return sum(b.launches for b in self.buckets.values())
 
+    @property
+    def graph_replays(self) -> int:
+        return sum(b.replays for b in self.buckets.values())
+
 
 def make_stream(count: int, seed: int, rate_hz: float, max_steps: int = 2000, min_steps: int = 100,
                 kmax: int = 8) -> List[SolveRequest]:
@@ -326,10 +372,14 @@ def make_stream(count: int, seed: int, rate_hz: float, max_steps: int = 2000, mi
     from . import initial
 
     rng = np.random.Generator(np.random.PCG64(seed))
+    # arrival gaps come from their own generator, so that the requests (kind, size, batch, steps,
+    # dt, initial field) are the same at every rate and a stream can be compared request by request
+    # with its burst (rate 0) or one-at-a-time run
+    arrivals = np.random.Generator(np.random.PCG64([seed, 1]))
     t = 0.0
     out = []
     for rid in range(count):
-        t += rng.exponential(1.0 / rate_hz) if rate_hz > 0 else 0.0
+        t += arrivals.exponential(1.0 / rate_hz) if rate_hz > 0 else 0.0
         if rng.integers(0, 2) == 0:
             kind, n, rms = "ks1d", int(rng.choice([256, 512, 1024, 2048, 4096])), 1.0
             shape = (n,)

@@ -598,12 +598,21 @@ def run_burgers2d_grad(args):
             op.integrate(u_0=u0d, dt=dt, step=steps)
             torch.cuda.synchronize()
             ftimes.append(time.perf_counter() - t0)
-    # FP32 central difference in nu through the fused forward
-    eps = 1e-3
-    with torch.no_grad():
-        lp = ((pde.Burgers(0.01 + eps).integrate(u_0=u0d, mesh=mesh, dt=dt, step=steps) - target) ** 2).mean().item()
-        lm = ((pde.Burgers(0.01 - eps).integrate(u_0=u0d, mesh=mesh, dt=dt, step=steps) - target) ** 2).mean().item()
-    fd = (lp - lm) / (2 * eps)
+    # FP32 central differences in nu through the fused forward; eps = 1e-3 is 10% of nu, so its
+    # O(eps^2) error is removed by Richardson extrapolation with eps / 2
+    def central(eps):
+        with torch.no_grad():
+            lp = ((pde.Burgers(0.01 + eps).integrate(u_0=u0d, mesh=mesh, dt=dt, step=steps) - target) ** 2).mean()
+            lm = ((pde.Burgers(0.01 - eps).integrate(u_0=u0d, mesh=mesh, dt=dt, step=steps) - target) ** 2).mean()
+        return (lp.item() - lm.item()) / (2 * eps)
+
+    fd1, fd2 = central(1e-3), central(5e-4)
+    fd = (4 * fd2 - fd1) / 3
+    ref = reference_autograd_burgers2d(dev, u0h, target, mesh, dt, steps)
+    if "grad_u0" in ref:
+        ref["rel_l2_grad_u0_vs_adjoint"] = float(torch.linalg.vector_norm(ref.pop("grad_u0") - gu.double())
+                                                 / torch.linalg.vector_norm(gu.double()))
+        ref["rel_diff_grad_nu_vs_adjoint"] = abs(ref["grad_nu"] - gnu) / abs(ref["grad_nu"])
     dof_steps = B * 2 * n * n * steps
     tb = statistics.median(times)
     tf = statistics.median(ftimes)
@@ -614,9 +623,50 @@ def run_burgers2d_grad(args):
             "config": {"workload": "burgers2d_grad_128x128_b16_500steps", "checkpoint_every": 50},
             "forward_only": {"value": dof_steps / tf, "ms": tf * 1e3},
             "backward_over_forward": tb / tf,
-            "gradients": {"loss": loss, "grad_nu_adjoint": gnu, "grad_nu_fd_fp32_eps1e-3": fd,
-                          "rel_diff": abs(gnu - fd) / abs(fd), "grad_u0_finite": bool(torch.isfinite(gu).all())}}
+            "gradients": {"loss": loss, "grad_nu_adjoint": gnu, "grad_nu_fd_fp32_eps1e-3": fd1,
+                          "grad_nu_fd_fp32_eps5e-4": fd2, "grad_nu_fd_richardson": fd,
+                          "rel_diff_vs_richardson": abs(gnu - fd) / abs(fd),
+                          "grad_u0_finite": bool(torch.isfinite(gu).all())},
+            "reference_autograd": ref}
     print(json.dumps(line))
+
+
+def reference_autograd_burgers2d(device, u0h, target, mesh, dt, steps) -> dict:
+    """The reference's own autograd gradient on the same GPU and inputs (FP32): nu * Laplacian() -
+    Convection() integrated by the unmodified reference installed under baseline/_ref, loss = MSE to
+    the same target, d loss / d u0 and d loss / d nu by loss.backward(); timed once."""
+    import torch
+
+    refdir = os.path.join(REPO, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(refdir, "torchfsm")):
+        return {"unavailable": "reference not installed under baseline/_ref"}
+    if refdir not in sys.path:
+        sys.path.insert(0, refdir)
+    try:
+        import torchfsm as R
+        from torchfsm.mesh import MeshGrid
+    except Exception as e:  # noqa: BLE001
+        return {"unavailable": f"reference import failed: {type(e).__name__}: {e}"}
+    m = MeshGrid(mesh, device=device)
+    nu = torch.tensor(0.01, device=device, requires_grad=True)
+    op = nu * R.operator.Laplacian() - R.operator.Convection()
+    # registers the mesh and builds the coefficients (with grad enabled, so that they depend on nu;
+    # no backward here, so their graph is still there for the timed backward)
+    op.integrate(u_0=u0h.to(device), mesh=m, dt=dt, step=1)
+    x = u0h.to(device).clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = op.integrate(u_0=x, dt=dt, step=steps)
+    loss = ((out - target) ** 2).mean()
+    loss.backward()
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    res = {"kind": "reference torch autograd (cuFFT + ATen), FP32", "seconds_fwd_bwd": t,
+           "loss": loss.item(), "grad_nu": nu.grad.item(), "grad_u0": x.grad.detach().double(),
+           "peak_mem_gb": torch.cuda.max_memory_allocated(device) / 1e9}
+    del out, loss, op, x
+    torch.cuda.empty_cache()
+    return res
 
 
 def ncu_case(workload: str = "ns2d"):

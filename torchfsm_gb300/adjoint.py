@@ -27,7 +27,8 @@ table derivatives come from the FP64 contour formulas (central differences
 in FP64).
 
 Spectral arithmetic of the backward pass runs as torch tensor operations on
-the GPU; every transform is the library's fsm_rfftn / fsm_irfftn.
+the GPU; every transform is the library's fsm_rfftn / fsm_irfftn. One adjoint
+step is captured as a CUDA graph and replayed for every step.
 """
 
 from __future__ import annotations
@@ -203,6 +204,34 @@ class ConvectionAdjoint:
         return total.reshape(total.shape[0], -1).sum(-1)
 
 
+class _StepGraph:
+    """One adjoint step (``ConvectionAdjoint.step_adjoint``: recomputed stages, vector-Jacobian
+    products, coefficient accumulation into ``tbar``) captured once as a CUDA graph and replayed
+    for every step; the step is a few hundred small launches, so the replay removes their host cost.
+    Inputs are copied into the graph's static buffers; the returned cotangent is the graph's
+    static output, valid until the next call."""
+
+    def __init__(self, adj: "ConvectionAdjoint", like: torch.Tensor, tbar):
+        dev = like.device
+        self.u_in = torch.zeros_like(like)
+        self.v_in = torch.zeros_like(like)
+        scratch = [torch.zeros_like(t) for t in tbar] if tbar is not None else None
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(torch.cuda.current_stream(dev))
+        with torch.cuda.stream(side):
+            adj.step_adjoint(self.u_in, self.v_in, scratch)  # warm-up: kernel attributes, allocator
+        torch.cuda.current_stream(dev).wait_stream(side)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.v_out = adj.step_adjoint(self.u_in, self.v_in, tbar)
+
+    def __call__(self, u: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+        self.u_in.copy_(u)
+        self.v_in.copy_(v)
+        self.graph.replay()
+        return self.v_out
+
+
 class _IntegrateFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, u0, adj, steps, checkpoint, symbols, *coefs):
@@ -233,6 +262,7 @@ class _IntegrateFn(torch.autograd.Function):
         tbar = None
         if want_coef:
             tbar = [torch.zeros(v.shape, dtype=torch.float64, device=v.device) for _ in range(6)]
+        step = _StepGraph(adj, v, tbar) if steps > 1 else None
         starts = list(range(0, steps, K))
         for si in reversed(range(len(starts))):
             start = starts[si]
@@ -242,7 +272,11 @@ class _IntegrateFn(torch.autograd.Function):
             frames = torch.empty((st.shape[0], n) + tuple(st.shape[1:]), dtype=torch.complex64, device=st.device)
             plan.integrate_half(st, n - 1, slots=list(range(n)), traj=frames) if n > 1 else frames[:, 0].copy_(st)
             for j in reversed(range(n)):
-                v = adj.step_adjoint(frames[:, j].contiguous(), v, tbar)
+                if step is not None:
+                    v = step(frames[:, j], v)
+                else:
+                    v = adj.step_adjoint(frames[:, j].contiguous(), v, tbar)
+        v = v.clone()
         grad_u0 = adj.ntot * adj.sp.to_physical(v) if ctx.needs_input_grad[0] else None
         grads = [None] * ctx.n_coefs
         if want_coef:

@@ -241,6 +241,47 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
             "B": B, "torch_ref": torch_ref}
 
 
+def _import_reference():
+    """The unmodified reference package installed under baseline/_ref, or (None, reason)."""
+    refdir = os.path.join(REPO, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(refdir, "torchfsm")):
+        return None, "reference not installed under baseline/_ref"
+    if refdir not in sys.path:
+        sys.path.insert(0, refdir)
+    try:
+        import torchfsm as R
+        import torchfsm.mesh  # noqa: F401
+        import torchfsm.pde  # noqa: F401
+        import torchfsm.traj_recorder  # noqa: F401
+    except Exception as e:  # noqa: BLE001
+        return None, f"reference import failed: {type(e).__name__}: {e}"
+    return R, None
+
+
+def reference_steady_step_ms(R, make_op, mesh, u, dt, k1: int, k2: int) -> dict:
+    """Steady per-step time of the reference's own integrate on the GPU: the difference of a k2-step
+    and a k1-step call (each call carries the reference's fixed gc/empty_cache cost), CUDA events."""
+    import torch
+
+    op = make_op(R)
+    m = R.mesh.MeshGrid(mesh, device=u.device)
+    op.integrate(u_0=u, mesh=m, dt=dt, step=1)  # registers the mesh, builds the coefficients
+
+    def timed(k):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        op.integrate(u_0=u, dt=dt, step=k)
+        e1.record()
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
+    t1, t2 = timed(k1), timed(k2)
+    return {"ms_per_step": (t2 - t1) / (k2 - k1), "steps_timed": [k1, k2], "call_ms": [t1, t2],
+            "kind": "reference torch path (cuFFT + ATen), FP32"}
+
+
 def torch_gpu_reference(device, w0: np.ndarray, ours_half=None, k1: int = 10, k2: int = 60) -> dict:
     """The reference's own torch path (cuFFT + ATen) on the same GPU, same config and inputs.
 
@@ -252,19 +293,11 @@ def torch_gpu_reference(device, w0: np.ndarray, ours_half=None, k1: int = 10, k2
     FP32 results is reported as well."""
     import torch
 
-    ref = os.path.join(REPO, "baseline", "_ref")
-    if not os.path.isdir(os.path.join(ref, "torchfsm")):
-        return {"unavailable": "reference not installed under baseline/_ref"}
-    if ref not in sys.path:
-        sys.path.insert(0, ref)
-    try:
-        import torchfsm as R
-        from torchfsm.mesh import MeshGrid
-        from torchfsm.pde import NavierStokesVorticity
-    except Exception as e:  # noqa: BLE001
-        return {"unavailable": f"reference import failed: {type(e).__name__}: {e}"}
-    mesh = MeshGrid(MESH, device=device)
-    op = NavierStokesVorticity(RE)
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    mesh = R.mesh.MeshGrid(MESH, device=device)
+    op = R.pde.NavierStokesVorticity(RE)
     u = torch.tensor(w0, device=device)
     u = u if u.dim() == 4 else u.unsqueeze(1)
     op.integrate(u_0=u, mesh=mesh, dt=DT, step=2)  # registers the mesh, builds the coefficients
@@ -401,6 +434,27 @@ def run_burgers1d(args):
                     record=lambda i: True, real_dtype=np.float32)
     cpu_s = (time.perf_counter() - t0) / reps
     p50 = _pctl(lat, 50)
+    # the reference's torch path on the same GPU: the same call (AutoRecorder, host in/out)
+    R, why = _import_reference()
+    if R is None:
+        torch_ref = {"unavailable": why}
+    else:
+        rop = R.pde.Burgers(0.01)
+        rmesh = R.mesh.MeshGrid(mesh, device=device)
+        rop.integrate(u_0=u0h.to(device), mesh=rmesh, dt=dt, step=1)
+        rl = []
+        for i in range(3 + 10):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rtraj = rop.integrate(u_0=u0h.to(device, non_blocking=True), dt=dt, step=steps,
+                                  trajectory_recorder=R.traj_recorder.AutoRecorder())
+            rtraj.cpu()
+            if i >= 3:
+                rl.append((time.perf_counter() - t0) * 1e3)
+        torch_ref = {"latency_ms": {"p50": _pctl(rl, 50), "p99": _pctl(rl, 99), "n": len(rl)},
+                     "value": n * steps / (_pctl(rl, 50) * 1e-3), "unit": "DOF*steps/s",
+                     "kind": "reference torch path (cuFFT + ATen), FP32, same call with AutoRecorder",
+                     "fused_e2e_over_reference": _pctl(rl, 50) / p50}
     line = {"metric": "DOF*steps/s (1D Burgers N=128, 200 SETDRK4 steps, 201 recorded frames)",
             "value": n * steps / (statistics.median(dev) * 1e-3), "unit": "DOF*steps/s", "n_gpus": 1,
             "steps": len(lat), "warmup": args.warmup, "ms_per_step": statistics.median(dev),
@@ -415,7 +469,8 @@ def run_burgers1d(args):
             "roofline": {"bound": "latency", "note": "one 128-point line per CTA; all 200 steps in one launch",
                          "device_ms": statistics.median(dev)},
             "cpu_baseline": {"value": n * steps / cpu_s, "unit": "DOF*steps/s", "cores": 1, "kind": "port",
-                             "sample": "the whole workload, numpy complex64 restatement, 1 thread"}}
+                             "sample": "the whole workload, numpy complex64 restatement, 1 thread"},
+            "torch_gpu_reference": torch_ref}
     print(json.dumps(line))
 
 
@@ -459,6 +514,17 @@ def run_burgers3d(args):
     dof_steps = 3 * n ** 3 * steps
     prof = profile_kernels(plan, state0, ws, device)
     finite = bool(torch.isfinite(torch.view_as_real(state)).all().item())
+    R, why = _import_reference()
+    if R is None:
+        torch_ref = {"unavailable": why}
+    else:
+        del ws
+        torch.cuda.empty_cache()
+        torch_ref = reference_steady_step_ms(R, lambda R: R.pde.Burgers(0.005), mesh, u0, dt, 1, 4)
+        torch_ref["value"] = 3 * n ** 3 / (torch_ref["ms_per_step"] * 1e-3)
+        torch_ref["unit"] = "DOF*steps/s"
+        torch_ref["fused_device_over_reference"] = (dof_steps / (ms * 1e-3)) / torch_ref["value"]
+        torch_ref["peak_mem_gb"] = torch.cuda.max_memory_allocated(device) / 1e9
     line = {"metric": "DOF*steps/s (3D Burgers 256^3 x 3 channels, SETDRK4, FP32)", "value": dof_steps / (ms * 1e-3),
             "unit": "DOF*steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/c64",
@@ -469,6 +535,7 @@ def run_burgers3d(args):
             "roofline": {"bound": "hbm", "per_kernel_ms": {k: v["avg_ms"] for k, v in prof.items() if v["launches"]},
                          "step_model_bytes_per_dof_step": 276,
                          "step_achieved_gbs": 276.0 * dof_steps / (ms * 1e-3) / 1e9, "peak": _peaks()[0]},
+            "torch_gpu_reference": torch_ref,
             "clocks": clk.summary()}
     print(json.dumps(line))
 
@@ -637,17 +704,10 @@ def reference_autograd_burgers2d(device, u0h, target, mesh, dt, steps) -> dict:
     the same target, d loss / d u0 and d loss / d nu by loss.backward(); timed once."""
     import torch
 
-    refdir = os.path.join(REPO, "baseline", "_ref")
-    if not os.path.isdir(os.path.join(refdir, "torchfsm")):
-        return {"unavailable": "reference not installed under baseline/_ref"}
-    if refdir not in sys.path:
-        sys.path.insert(0, refdir)
-    try:
-        import torchfsm as R
-        from torchfsm.mesh import MeshGrid
-    except Exception as e:  # noqa: BLE001
-        return {"unavailable": f"reference import failed: {type(e).__name__}: {e}"}
-    m = MeshGrid(mesh, device=device)
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    m = R.mesh.MeshGrid(mesh, device=device)
     nu = torch.tensor(0.01, device=device, requires_grad=True)
     op = nu * R.operator.Laplacian() - R.operator.Convection()
     # registers the mesh and builds the coefficients (with grad enabled, so that they depend on nu;

@@ -71,6 +71,18 @@ extern "C" {
 #define FSM_SETDRK2 12
 #define FSM_SETDRK3 13
 #define FSM_SETDRK4 14
+/* explicit Runge-Kutta on the full right-hand side L u + N(u), fixed step
+   (integrator/_rk.py:43-58 _rk_step; tableaus :82-255) */
+#define FSM_RK_EULER 21
+#define FSM_RK_MIDPOINT 22
+#define FSM_RK_HEUN12 23
+#define FSM_RK_RALSTON12 24
+#define FSM_RK_BOGACKI_SHAMPINE23 25
+#define FSM_RK4 26
+#define FSM_RK4_38RULE 27
+#define FSM_RK_DORPI45 28
+#define FSM_RK_FEHLBERG45 29
+#define FSM_RK_CASHKARP45 30
 
 typedef struct FsmPlan FsmPlan;
 
@@ -84,7 +96,7 @@ typedef struct FsmProgramDesc {
   int32_t n_channel;
   int32_t nonlinear;        /* FSM_NL_* */
   int32_t flags;            /* FSM_FLAG_* */
-  int32_t integrator;       /* FSM_ETDRK* / FSM_SETDRK* */
+  int32_t integrator;       /* FSM_ETDRK* / FSM_SETDRK* / FSM_RK* */
   double nonlinear_coef;    /* scalar coefficient of the nonlinear term */
   const uint8_t* keep[3];   /* HOST: per axis, n[i] dealias keep flags in fftfreq order
                                (mesh.py:443-461); NULL keeps every mode */

@@ -289,6 +289,11 @@ def stage_step(name: str, tabs: dict, nonlinear: Callable, u: np.ndarray) -> np.
 
     setdrk1..4: _stable_etdrk/_setdrk_step.py:5-82; etdrk0..2: _etdrk.py:22-82.
     """
+    if name in RK_TABLEAUS:
+        # f(u) = L u + N(u) (operator/_base.py:408-431)
+        L = tabs["L"]
+        rhs = (lambda x: L * x) if nonlinear is None else (lambda x: L * x + nonlinear(x))
+        return rk_step(name, rhs, u, tabs["dt"])
     E = tabs["E"]
     if name == "etdrk0":
         return E * u
@@ -325,7 +330,47 @@ def stage_step(name: str, tabs: dict, nonlinear: Callable, u: np.ndarray) -> np.
     raise ValueError(name)
 
 
+# Explicit Runge-Kutta tableaus by the reference's enum names (integrator/_rk.py:82-255):
+# (rows of [c_i, a_i0, a_i1, ...] for the stages after the first, weights b).
+RK_TABLEAUS = {
+    "Euler": ([[1.0]], [1.0]),
+    "Midpoint": ([[1 / 2, 1 / 2]], [0, 1]),
+    "Heun12": ([[1, 1]], [1 / 2, 1 / 2]),
+    "Ralston12": ([[2 / 3, 2 / 3]], [1 / 4, 3 / 4]),
+    "BogackiShampine23": ([[1 / 2, 1 / 2], [3 / 4, 0, 3 / 4], [1, 2 / 9, 1 / 3, 4 / 9]], [2 / 9, 1 / 3, 4 / 9, 0]),
+    "RK4": ([[1 / 2, 1 / 2], [1 / 2, 0, 1 / 2], [1, 0, 0, 1]], [1 / 6, 1 / 3, 1 / 3, 1 / 6]),
+    # the last row, read with the first entry as c like every other row, gives a3 = (-1, 1, 1)
+    # (the textbook 3/8 rule has (1, -1, 1)): the reference runs it that way, and so does this
+    "RK4_38Rule": ([[1 / 3, 1 / 3], [2 / 3, -1 / 3, 1], [1, -1, 1, 1]], [1 / 8, 3 / 8, 3 / 8, 1 / 8]),
+    "Dorpi45": ([[1 / 5, 1 / 5], [3 / 10, 3 / 40, 9 / 40], [4 / 5, 44 / 45, -56 / 15, 32 / 9],
+                 [8 / 9, 19372 / 6561, -25360 / 2187, 64448 / 6561, -212 / 729],
+                 [1, 9017 / 3168, -355 / 33, 46732 / 5247, 49 / 176, -5103 / 18656],
+                 [1, 35 / 384, 0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84]],
+                [35 / 384, 0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84]),
+    "Fehlberg45": ([[1 / 4, 1 / 4], [3 / 8, 3 / 32, 9 / 32], [12 / 13, 1932 / 2197, -7200 / 2197, 7296 / 2197],
+                    [1, 439 / 216, -8, 3680 / 513, -845 / 4104], [1 / 2, -8 / 27, 2, -3544 / 2565, 1859 / 4104, -11 / 40]],
+                   [16 / 135, 0, 6656 / 12825, 28561 / 56430, -9 / 50, 2 / 55]),
+    "CashKarp45": ([[1 / 5, 1 / 5], [3 / 10, 3 / 40, 9 / 40], [3 / 5, 3 / 10, -9 / 10, 6 / 5],
+                    [1, -11 / 54, 5 / 2, -70 / 27, 35 / 27],
+                    [7 / 8, 1631 / 55296, 175 / 512, 575 / 13824, 44275 / 110592, 253 / 4096]],
+                   [37 / 378, 0, 250 / 621, 125 / 594, 0, 512 / 1771]),
+}
+
+
+def rk_step(name: str, rhs: Callable, x: np.ndarray, dt: float) -> np.ndarray:
+    """One fixed step of an explicit Runge-Kutta scheme (integrator/_rk.py:43-58, _rk_step):
+    k_0 = f(x), k_{i+1} = f(x + dt sum_j a_ij k_j), x' = x + dt sum_i b_i k_i (sums truncated to the
+    slopes available, as the reference's zip does)."""
+    ca, b = RK_TABLEAUS[name]
+    ks = [rhs(x)]
+    for row in ca:
+        ks.append(rhs(x + dt * sum(a * k for a, k in zip(row[1:], ks))))
+    return x + dt * sum(w * k for w, k in zip(b, ks))
+
+
 def build_tables(name: str, lin: np.ndarray, dt: float, m: int = 16, r: float = 1.0) -> dict:
+    if name in RK_TABLEAUS:
+        return {"L": np.asarray(lin), "dt": dt}
     if name.startswith("setdrk"):
         return setdrk_coefs(int(name[-1]), lin, dt, m, r)
     return etdrk_coefs(int(name[-1]), lin, dt)
@@ -367,7 +412,8 @@ def integrate(
     if integrator == "auto":
         integrator = "etdrk0" if nonlinear is None else "setdrk4"
     tabs = build_tables(integrator, lin, dt, n_integration_points, integration_radius)
-    tabs = {k: np.asarray(v).astype(mesh.complex_dtype if np.iscomplexobj(v) else mesh.real_dtype) for k, v in tabs.items()}
+    tabs = {k: (v if k == "dt" else np.asarray(v).astype(mesh.complex_dtype if np.iscomplexobj(v) else mesh.real_dtype))
+            for k, v in tabs.items()}
     u_hat = mesh.fft(u0.astype(real_dtype)) if u0_fft is None else u0_fft.astype(mesh.complex_dtype)
     frames: List[np.ndarray] = []
     for i in range(step):

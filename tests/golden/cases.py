@@ -198,6 +198,62 @@ for _name in ("setdrk1", "setdrk2", "setdrk3", "etdrk1", "etdrk2"):
         ic=_sin_plus_half,
     )
 
+# Explicit Runge-Kutta integrators (integrator/_rk.py), fixed step: every tableau on 1D Burgers
+# (32 points, so that |dt L| <= 1 stays inside every scheme's stability region), and RK on the
+# other fused paths: 2D plane passes, vorticity, 3D volume passes, the linear pointwise kernel,
+# and the 1D KS batch-mean fix-up.
+RK_NAMES = ("Euler", "Midpoint", "Heun12", "Ralston12", "BogackiShampine23", "RK4", "RK4_38Rule", "Dorpi45",
+            "Fehlberg45", "CashKarp45")
+for _name in RK_NAMES:
+    CASES[f"burgers1d_rk_{_name.lower()}"] = dict(
+        mesh=[(0, 1, 32)], batch=2, channels=1, dt=0.005, step=50, record=10,
+        build=lambda M: M.pde.Burgers(0.02), integrator=_name,
+        lin=[(0.02, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(171, (32,), 4, 0.5),
+    )
+CASES.update({
+    "burgers2d_rk4_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=2, dt=0.01, step=20, record=5,
+        build=lambda M: M.pde.Burgers(0.01), integrator="RK4",
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(181, (32, 32), 4, 0.5),
+    ),
+    "ns2d_dorpi45_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=1, dt=0.01, step=20, record=0,
+        build=lambda M: M.pde.NavierStokesVorticity(1000), integrator="Dorpi45",
+        lin=[(1.0 / 1000, ("laplacian",))], nl=[(-1.0, "vorticity_convection")],
+        ic=_grf2(191, 32),
+    ),
+    "burgers3d_fehlberg45_n16": dict(
+        mesh=[(0, TWO_PI, 16)] * 3, batch=1, channels=3, dt=0.01, step=8, record=0,
+        build=lambda M: M.pde.Burgers(0.005), integrator="Fehlberg45",
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_grf3(201, 16),
+    ),
+    "heat2d_rk4": dict(
+        mesh=[(0, 1, 32), (0, 1, 32)], batch=2, channels=1, dt=0.001, step=10, record=1,
+        build=lambda M: 0.05 * M.operator.Laplacian(), integrator="RK4",
+        lin=[(0.05, ("laplacian",))], nl=[],
+        ic=_bl(211, (32, 32), 5, 1.0),
+    ),
+    "ksnd1d_b3_rk438": dict(
+        mesh=[(0, 10 * math.pi, 64)], batch=3, channels=1, dt=0.001, step=40, record=8,
+        build=lambda M: M.pde.KuramotoSivashinskyHighDim(), integrator="RK4_38Rule",
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")],
+        ic=_bl(221, (64,), 6, 0.7),
+    ),
+})
+
+
+def set_case_integrator(op, M, kind):
+    """Select a case's integrator by name on a torchfsm-like namespace."""
+    if kind in RK_NAMES:
+        op.set_integrator(M.integrator.RKIntegrator[kind])
+    elif kind.startswith("setdrk"):
+        op.set_integrator(M.integrator.SETDRKIntegrator[kind.upper()])
+    else:
+        op.set_integrator(M.integrator.ETDRKIntegrator[kind.upper()])
+
 
 def initial_condition(name: str) -> np.ndarray:
     c = CASES[name]

@@ -57,7 +57,7 @@ def main(ref_root: str) -> None:
         u0 = C.initial_condition(name)
         op = case["build"](M)
         if case.get("integrator"):
-            op.set_integrator(enums[case["integrator"]])
+            C.set_case_integrator(op, M, case["integrator"])
         rec_fn = C.record_fn(name)
         rec = AutoRecorder(control_func=rec_fn) if rec_fn is not None else None
         out = op.integrate(

@@ -28,9 +28,7 @@ def _run(name, device="cuda", dtype=torch.float32):
     M = C.namespace("torchfsm_gb300")
     op = case["build"](M)
     if case.get("integrator"):
-        kind = case["integrator"]
-        enum = M.integrator.SETDRKIntegrator if kind.startswith("setdrk") else M.integrator.ETDRKIntegrator
-        op.set_integrator(enum[kind.upper()])
+        C.set_case_integrator(op, M, case["integrator"])
     u0 = torch.tensor(C.initial_condition(name), dtype=dtype, device=device)
     rec_fn = C.record_fn(name)
     rec = M.traj_recorder.AutoRecorder(control_func=rec_fn) if rec_fn is not None else None

@@ -74,3 +74,17 @@ def test_linear_symbol_fp64_matches_oracle(name):
     ref = S.linear_symbol(S.OMesh(case["mesh"]), case["lin"], case["channels"])
     L = np.broadcast_to(L, np.broadcast_shapes(L.shape, ref.shape))
     np.testing.assert_allclose(L, np.broadcast_to(ref, L.shape), rtol=1e-12, atol=1e-9)
+
+
+def test_rk_integrators_select_fixed_step_schemes_and_refuse_adaptive():
+    from torchfsm_gb300 import pde
+    from torchfsm_gb300.integrator import RKIntegrator
+
+    op = pde.Burgers(0.01)
+    for member in RKIntegrator:
+        op.set_integrator(member)
+        assert op._integrator_id() == member.value
+        assert _lib.FSM_RK_EULER <= member.value <= _lib.FSM_RK_CASHKARP45
+    op.set_integrator(RKIntegrator.Dorpi45, adaptive=True, atol=1e-6, rtol=1e-5)
+    with pytest.raises(NotImplementedError):
+        op._integrator_id()

@@ -39,6 +39,16 @@ FSM_SETDRK1 = 11
 FSM_SETDRK2 = 12
 FSM_SETDRK3 = 13
 FSM_SETDRK4 = 14
+FSM_RK_EULER = 21
+FSM_RK_MIDPOINT = 22
+FSM_RK_HEUN12 = 23
+FSM_RK_RALSTON12 = 24
+FSM_RK_BOGACKI_SHAMPINE23 = 25
+FSM_RK4 = 26
+FSM_RK4_38RULE = 27
+FSM_RK_DORPI45 = 28
+FSM_RK_FEHLBERG45 = 29
+FSM_RK_CASHKARP45 = 30
 
 # Every symbol the header declares; tests check that the library exports them.
 EXPORTS = (

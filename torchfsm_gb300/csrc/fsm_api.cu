@@ -86,6 +86,12 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
   const int64_t idx = first + k;
   const cd l = L ? mk(L[idx % lcount].x, L[idx % lcount].y) : mk(0.0, 0.0);
   const cd hl = dt * l;
+  if (is_rk(integ)) {
+    // explicit Runge-Kutta slopes dt (L a + N): the tables are dt L and dt
+    tab[idx] = tof(hl);
+    tab[ts + idx] = make_float2((float)dt, 0.f);
+    return;
+  }
   const cd E = cexpd(hl);
   tab[idx] = tof(E);
   if (integ == FSM_ETDRK0) return;
@@ -190,7 +196,7 @@ __global__ void k_pointwise(StepArgs a, int64_t total) {
     const int c = (int)((idx / S) % C);
     const int b = (int)(idx / (S * C));
     float2 u = a.state[idx];
-    float2 acc = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
+    float2 aux[6] = {};  // scheme running sums (acc, q; Runge-Kutta partial inputs)
     const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + s;
     const float2* tab = a.tab + toff;
     const float2 nv = a.src ? a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + s] : make_float2(0.f, 0.f);
@@ -200,7 +206,7 @@ __global__ void k_pointwise(StepArgs a, int64_t total) {
       if (a.integ == FSM_ETDRK0) {
         u = cmul(tab[0], u);
       } else {
-        for (int st = 0; st < a.nstages; ++st) (void)etd_stage(a.integ, st, nv, &u, &acc, &q, tab, a.ts);
+        for (int st = 0; st < a.nstages; ++st) (void)etd_stage(a.integ, st, nv, &u, aux, aux + 1, tab, a.ts, 1);
       }
       const int slot = a.slots ? a.slots[step + 1] : -1;
       if (slot >= 0) a.traj[(((int64_t)b * a.n_frames + slot) * C + c) * S + s] = u;

@@ -15,7 +15,71 @@ constexpr int kTwiddleMax = 4096;  // master twiddle table W_4096^k
 constexpr int kMaxTables = 7;
 
 // Number of nonlinear evaluations per step of each scheme.
+// Explicit Runge-Kutta tableaus (integrator/_rk.py:82-255), stages that feed the step only:
+// a[i][j] weighs stage j's slope in the input of stage i (j < i), b[i] in the new state. The
+// reference evaluates one more slope for Euler (a zero-weight repeat) and for BogackiShampine23
+// and Dorpi45 (the first-same-as-last stage, used only by the adaptive error estimate); those
+// evaluations do not enter the fixed-step result and are not run here.
+struct RKTableau {
+  int s;
+  float a[6][6];
+  float b[6];
+};
+
+__host__ __device__ constexpr bool is_rk(int integ) { return integ >= FSM_RK_EULER && integ <= FSM_RK_CASHKARP45; }
+
+__host__ __device__ constexpr RKTableau rk_tableau(int integ) {
+  switch (integ) {
+    case FSM_RK_EULER: return {1, {{0}}, {1.f}};
+    case FSM_RK_MIDPOINT: return {2, {{0}, {0.5f}}, {0.f, 1.f}};
+    case FSM_RK_HEUN12: return {2, {{0}, {1.f}}, {0.5f, 0.5f}};
+    case FSM_RK_RALSTON12: return {2, {{0}, {2.f / 3.f}}, {0.25f, 0.75f}};
+    case FSM_RK_BOGACKI_SHAMPINE23: return {3, {{0}, {0.5f}, {0.f, 0.75f}}, {2.f / 9.f, 1.f / 3.f, 4.f / 9.f}};
+    case FSM_RK4: return {4, {{0}, {0.5f}, {0.f, 0.5f}, {0.f, 0.f, 1.f}}, {1.f / 6.f, 1.f / 3.f, 1.f / 3.f, 1.f / 6.f}};
+    case FSM_RK4_38RULE:
+      // the reference's last row [1, -1, 1, 1] read as [c, a30, a31, a32] gives a3 = (-1, 1, 1)
+      // (the textbook 3/8 rule has (1, -1, 1)); kept as the reference runs it
+      return {4, {{0}, {1.f / 3.f}, {-1.f / 3.f, 1.f}, {-1.f, 1.f, 1.f}}, {0.125f, 0.375f, 0.375f, 0.125f}};
+    case FSM_RK_DORPI45:
+      return {6,
+              {{0},
+               {1.f / 5.f},
+               {3.f / 40.f, 9.f / 40.f},
+               {44.f / 45.f, -56.f / 15.f, 32.f / 9.f},
+               {19372.f / 6561.f, -25360.f / 2187.f, 64448.f / 6561.f, -212.f / 729.f},
+               {9017.f / 3168.f, -355.f / 33.f, 46732.f / 5247.f, 49.f / 176.f, -5103.f / 18656.f}},
+              {35.f / 384.f, 0.f, 500.f / 1113.f, 125.f / 192.f, -2187.f / 6784.f, 11.f / 84.f}};
+    case FSM_RK_FEHLBERG45:
+      return {6,
+              {{0},
+               {1.f / 4.f},
+               {3.f / 32.f, 9.f / 32.f},
+               {1932.f / 2197.f, -7200.f / 2197.f, 7296.f / 2197.f},
+               {439.f / 216.f, -8.f, 3680.f / 513.f, -845.f / 4104.f},
+               {-8.f / 27.f, 2.f, -3544.f / 2565.f, 1859.f / 4104.f, -11.f / 40.f}},
+              {16.f / 135.f, 0.f, 6656.f / 12825.f, 28561.f / 56430.f, -9.f / 50.f, 2.f / 55.f}};
+    case FSM_RK_CASHKARP45:
+      return {6,
+              {{0},
+               {1.f / 5.f},
+               {3.f / 40.f, 9.f / 40.f},
+               {3.f / 10.f, -9.f / 10.f, 6.f / 5.f},
+               {-11.f / 54.f, 5.f / 2.f, -70.f / 27.f, 35.f / 27.f},
+               {1631.f / 55296.f, 175.f / 512.f, 575.f / 13824.f, 44275.f / 110592.f, 253.f / 4096.f}},
+              {37.f / 378.f, 0.f, 250.f / 621.f, 125.f / 594.f, 0.f, 512.f / 1771.f}};
+  }
+  return {0, {{0}}, {0}};
+}
+
+// The tableaus in constant memory for the kernels (indexed by integ - FSM_RK_EULER).
+static __constant__ RKTableau kRKTab[10] = {
+    rk_tableau(FSM_RK_EULER),   rk_tableau(FSM_RK_MIDPOINT),       rk_tableau(FSM_RK_HEUN12),
+    rk_tableau(FSM_RK_RALSTON12), rk_tableau(FSM_RK_BOGACKI_SHAMPINE23), rk_tableau(FSM_RK4),
+    rk_tableau(FSM_RK4_38RULE), rk_tableau(FSM_RK_DORPI45),         rk_tableau(FSM_RK_FEHLBERG45),
+    rk_tableau(FSM_RK_CASHKARP45)};
+
 __host__ __device__ inline int scheme_stages(int integ) {
+  if (is_rk(integ)) return rk_tableau(integ).s;
   switch (integ) {
     case FSM_SETDRK4: return 4;
     case FSM_SETDRK3: return 3;
@@ -34,6 +98,7 @@ __host__ __device__ inline int scheme_stages(int integ) {
 //  SETDRK1 / ETDRK1: E, c1
 //  ETDRK0: E
 __host__ __device__ inline int scheme_tables(int integ) {
+  if (is_rk(integ)) return 2;  // dt L, dt
   switch (integ) {
     case FSM_SETDRK4: return 6;
     case FSM_SETDRK3: return 7;
@@ -48,6 +113,10 @@ __host__ __device__ inline int scheme_tables(int integ) {
 
 // Auxiliary per-point state arrays a scheme keeps between stages (acc, q).
 __host__ __device__ inline int scheme_aux(int integ) {
+  if (is_rk(integ)) {
+    const int st = rk_tableau(integ).s;
+    return st > 1 ? st : 0;  // partial inputs of stages 1..s-1 and the weighted slope sum
+  }
   switch (integ) {
     case FSM_SETDRK4:
     case FSM_SETDRK3: return 2;
@@ -137,10 +206,55 @@ __device__ __forceinline__ float2 etd_stage_c(float2 nv, float2* __restrict__ u,
   }
 }
 
-// Run-time dispatch onto etd_stage_c.
+// One explicit Runge-Kutta stage at one point (integrator/_rk.py:43-58 with f = L u + N(u),
+// operator/_base.py:408-431). Slopes are kept scaled by dt: K = (dt L) a + dt N(a), from the
+// tables dt L (tab[0]) and dt (tab[ts].x). aux[j * astride] holds, for j < s-1, the partial
+// input P_{j+1} = sum_i a[j+1][i] K_i of stage j+1 and, at j = s-1, the sum B = sum_i b[i] K_i.
+// Stage i reads the state u and P_i (a_i = u + P_i), adds its slope to every later partial
+// input and to B, and returns a_{i+1}; the last stage writes u + B + b[s-1] K to u.
+__device__ __forceinline__ float2 rk_stage(int integ, int i, float2 nv, float2* __restrict__ u,
+                                           float2* __restrict__ aux, int64_t astride,
+                                           const float2* __restrict__ tab, int64_t ts) {
+  const RKTableau& T = kRKTab[integ - FSM_RK_EULER];
+  const float2 uu = *u;
+  const float2 a = (i == 0) ? uu : cadd(uu, aux[(int64_t)(i - 1) * astride]);
+  const float dt = tab[ts].x;
+  const float2 K = cfma(tab[0], a, cscale(nv, dt));
+  if (i == T.s - 1) {
+    float2 un = cadd(uu, cscale(K, T.b[i]));
+    if (i > 0) un = cadd(un, aux[(int64_t)(T.s - 1) * astride]);
+    *u = un;
+    return un;
+  }
+  float2 next = uu;
+  for (int m = i + 1; m < T.s; ++m) {
+    float2* pm = aux + (int64_t)(m - 1) * astride;
+    const float w = T.a[m][i];
+    float2 p;
+    if (i == 0) {
+      p = cscale(K, w);
+      *pm = p;
+    } else if (w != 0.f) {
+      p = cfma(make_float2(w, 0.f), K, *pm);
+      *pm = p;
+    } else if (m == i + 1) {
+      p = *pm;
+    } else {
+      continue;
+    }
+    if (m == i + 1) next = cadd(uu, p);
+  }
+  float2* pb = aux + (int64_t)(T.s - 1) * astride;
+  *pb = (i == 0) ? cscale(K, T.b[i]) : cfma(make_float2(T.b[i], 0.f), K, *pb);
+  return next;
+}
+
+// Run-time dispatch onto etd_stage_c / rk_stage. `astride` is the distance between the
+// Runge-Kutta aux arrays (acc is the first of them); the exponential schemes use acc and q.
 __device__ __forceinline__ float2 etd_stage(int integ, int s, float2 nv, float2* __restrict__ u,
                                             float2* __restrict__ acc, float2* __restrict__ q,
-                                            const float2* __restrict__ tab, int64_t ts) {
+                                            const float2* __restrict__ tab, int64_t ts, int64_t astride = 0) {
+  if (is_rk(integ)) return rk_stage(integ, s, nv, u, acc, astride, tab, ts);
   switch (integ) {
     case FSM_SETDRK4:
       switch (s) {

@@ -18,7 +18,8 @@ struct LineCfg {
   static constexpr int G = (N / 16 < 32) ? 32 : N / 16;
   static constexpr bool BLOCK = G > 32;
   static constexpr int H = N / 2 + 1;
-  static constexpr size_t SMEM = (size_t)(2 * N + 3 * H) * sizeof(float2);
+  // twiddles, transform buffer, state and the scheme's running sums (at least acc and q)
+  static size_t smem(int n_aux) { return (size_t)(2 * N + (1 + (n_aux > 2 ? n_aux : 2)) * H) * sizeof(float2); }
 };
 
 // Build the inverse-transform input of the stage field `a` at index k.
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
   float2* tw = smem;
   float2* Z = tw + N;
   float2* u = Z + N;
-  float2* acc = u + H;
+  float2* acc = u + H;  // running sums: acc, q (Runge-Kutta: n_aux arrays H apart)
   float2* q = acc + H;
   const int b = blockIdx.x;
   const int t = threadIdx.x;
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
         if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && k == 0)
           a.dc[((int64_t)step * ns + s) * a.B + b] = Z[0];
         if (src) nv = cadd(nv, src[k]);
-        const float2 nxt = etd_stage(a.integ, s, nv, u + k, acc + k, q + k, tab + k, a.ts);
+        const float2 nxt = etd_stage(a.integ, s, nv, u + k, acc + k, q + k, tab + k, a.ts, H);
         if (!final_stage) line_build<N, KIND>(Z, k, nxt, (float)a.keepx[k], a.kx[k], a.scale);
         if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H + k] = u[k];
       }
@@ -103,9 +104,10 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
 template <int N, int KIND>
 static int launch_line_n(const StepArgs& a, cudaStream_t st) {
   using Cfg = LineCfg<N>;
-  int rc = prep_smem(k_line<N, KIND>, Cfg::SMEM);
+  const size_t smem = Cfg::smem(a.n_aux);
+  int rc = prep_smem(k_line<N, KIND>, smem);
   if (rc) return rc;
-  k_line<N, KIND><<<a.B, Cfg::G, Cfg::SMEM, st>>>(a);
+  k_line<N, KIND><<<a.B, Cfg::G, smem, st>>>(a);
   return cuda_check(cudaGetLastError(), "k_line");
 }
 
@@ -158,14 +160,14 @@ __global__ void k_line_dc_fixup(StepArgs a) {
   const int H = a.H;
   const float2* mean = a.dc + (int64_t)a.steps * ns * a.B + a.B;
   float2 u = a.dc[(int64_t)a.steps * ns * a.B + b];
-  float2 acc = make_float2(0.f, 0.f), q = make_float2(0.f, 0.f);
+  float2 aux[6] = {};  // the scheme's running sums at k = 0
   const float2* tab = a.tab + (int64_t)(a.lin_batch > 1 ? b : 0) * H;
   const float2 src0 = a.src ? a.src[(int64_t)(a.src_batch > 1 ? b : 0) * H] : make_float2(0.f, 0.f);
   for (int step = 0; step < a.steps; ++step) {
     for (int s = 0; s < ns; ++s) {
       const int64_t row = (int64_t)step * ns + s;
       const float2 nv = cadd(cscale(csub(a.dc[row * a.B + b], mean[row]), a.coef), src0);
-      (void)etd_stage(a.integ, s, nv, &u, &acc, &q, tab, a.ts);
+      (void)etd_stage(a.integ, s, nv, &u, aux, aux + 1, tab, a.ts, 1);
     }
     const int slot = a.slots ? a.slots[step + 1] : -1;
     if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H] = u;

@@ -163,7 +163,7 @@ __device__ __forceinline__ void axis0_update(const StepArgs& a, float2* __restri
         if (STG >= 0)
           st = etd_stage_c<INTEG, STG>(nv[f], up, accp, qp, tab + toff, a.ts);
         else
-          st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, tab + toff, a.ts);
+          st = etd_stage(a.integ, a.stage, nv[f], up, accp, qp, tab + toff, a.ts, (int64_t)C * S);
       }
       if (a.slot >= 0 && (!update || last)) traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + sidx] = st;
       tileA[(f * W + col) * P + row] = cscale(st, pk.mask);

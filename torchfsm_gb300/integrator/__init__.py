@@ -6,8 +6,11 @@ and ``SETDRKIntegrator.SETDRK1..4`` (Kassam-Trefethen contour coefficients,
 integrator/_stable_etdrk/). ``set_integrator(enum, n_integration_points=..,
 integration_radius=.., cpu_cached=..)`` accepts the reference's options;
 ``cpu_cached`` is accepted and ignored (coefficients are always evaluated on
-the device in FP64). ``RKIntegrator`` (explicit Runge-Kutta) is listed for
-API compatibility; selecting it raises NotImplementedError.
+the device in FP64). ``RKIntegrator`` members select the explicit Runge-Kutta
+schemes of integrator/_rk.py with a fixed step on the full right-hand side
+L u + N(u) (operator/_base.py:408-431, 492-502); ``adaptive=True`` (step-size
+control by an error estimate with a host decision per trial step,
+integrator/_rk.py:60-79) is not provided and raises NotImplementedError.
 """
 
 from enum import Enum
@@ -29,16 +32,16 @@ class SETDRKIntegrator(Enum):
 
 
 class RKIntegrator(Enum):
-    Euler = "Euler"
-    Midpoint = "Midpoint"
-    Heun12 = "Heun12"
-    Ralston12 = "Ralston12"
-    BogackiShampine23 = "BogackiShampine23"
-    RK4 = "RK4"
-    RK4_38Rule = "RK4_38Rule"
-    Dorpi45 = "Dorpi45"
-    Fehlberg45 = "Fehlberg45"
-    CashKarp45 = "CashKarp45"
+    Euler = _lib.FSM_RK_EULER
+    Midpoint = _lib.FSM_RK_MIDPOINT
+    Heun12 = _lib.FSM_RK_HEUN12
+    Ralston12 = _lib.FSM_RK_RALSTON12
+    BogackiShampine23 = _lib.FSM_RK_BOGACKI_SHAMPINE23
+    RK4 = _lib.FSM_RK4
+    RK4_38Rule = _lib.FSM_RK4_38RULE
+    Dorpi45 = _lib.FSM_RK_DORPI45
+    Fehlberg45 = _lib.FSM_RK_FEHLBERG45
+    CashKarp45 = _lib.FSM_RK_CASHKARP45
 
 
 __all__ = ["ETDRKIntegrator", "SETDRKIntegrator", "RKIntegrator"]

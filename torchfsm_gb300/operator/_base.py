@@ -306,7 +306,7 @@ class OperatorLike(_MutableMixIn):
         self.coefs.append(coef)
 
     def set_integrator(self, integrator, **integrator_config):
-        """"auto", an ETDRKIntegrator or a SETDRKIntegrator member (operator/_base.py:646-674)."""
+        """"auto", an ETDRKIntegrator, SETDRKIntegrator or RKIntegrator member (operator/_base.py:646-674)."""
         if isinstance(integrator, str):
             assert integrator == "auto", \
                 "The integrator should be 'auto' or an instance of ETDRKIntegrator, SETDRKIntegrator or RKIntegrator"
@@ -322,9 +322,9 @@ class OperatorLike(_MutableMixIn):
     def _integrator_id(self) -> int:
         if self._integrator == "auto":
             return _lib.FSM_ETDRK0 if self.is_linear else _lib.FSM_SETDRK4
-        if isinstance(self._integrator, RKIntegrator):
-            raise NotImplementedError("explicit Runge-Kutta integrators are not provided by torchfsm_gb300; "
-                                      "use an ETDRKIntegrator or SETDRKIntegrator")
+        if isinstance(self._integrator, RKIntegrator) and self._integrator_config.get("adaptive", False):
+            raise NotImplementedError("adaptive step-size control of the Runge-Kutta integrators is not provided "
+                                      "by torchfsm_gb300; the fixed-step schemes are")
         return int(self._integrator.value)
 
     @torch.no_grad()

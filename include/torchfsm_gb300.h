@@ -83,6 +83,9 @@ extern "C" {
 #define FSM_RK_DORPI45 28
 #define FSM_RK_FEHLBERG45 29
 #define FSM_RK_CASHKARP45 30
+/* one evaluation of the right-hand side: a 1-step integrate overwrites the state with
+   L u + N(u) (Operator.__call__, operator/_base.py:753-790) */
+#define FSM_APPLY 40
 
 typedef struct FsmPlan FsmPlan;
 

@@ -436,3 +436,17 @@ def rel_l2(a: np.ndarray, b: np.ndarray) -> float:
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def apply_operator(u: np.ndarray, mesh_info, linear_terms, nonlinear_terms, de_aliasing_rate: float = 2.0 / 3.0,
+                   real_dtype=np.float64) -> np.ndarray:
+    """One evaluation ifft(L u_hat + N(u_hat)).real (operator/_base.py:408-431, 753-790)."""
+    mesh = OMesh(mesh_info, real_dtype)
+    u_hat = mesh.fft(np.asarray(u, dtype=real_dtype))
+    out = np.zeros_like(u_hat)
+    if linear_terms:
+        out = out + linear_symbol(mesh, linear_terms, u.shape[1]) * u_hat
+    nonlinear = make_nonlinear(mesh, nonlinear_terms, de_aliasing_rate)
+    if nonlinear is not None:
+        out = out + nonlinear(u_hat)
+    return mesh.ifft(out).real

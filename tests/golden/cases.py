@@ -291,6 +291,7 @@ def namespace(module_root):
         pde=importlib.import_module(module_root + ".pde"),
         operator=importlib.import_module(module_root + ".operator"),
         integrator=importlib.import_module(module_root + ".integrator"),
+        functional=importlib.import_module(module_root + ".functional"),
         traj_recorder=importlib.import_module(module_root + ".traj_recorder"),
         torch=torch,
     )
@@ -311,4 +312,63 @@ GRAD_CASES = {
 
 def grad_initial_condition(name: str) -> np.ndarray:
     c = GRAD_CASES[name]
+    return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)
+
+
+# One-shot evaluation (Operator.__call__, LinearOperator.solve, functional.*): fn(M, u, mesh) on a
+# float64 field; programs the library lowers run fused (the FSM_APPLY scheme), the
+# channel-changing post-processing cores through torch spectral multiplies.
+APPLY_CASES = {
+    "apply_burgers2d_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(231, (32, 32), 6, 1.0), batch=2, channels=2,
+                                fn=lambda M, u, m: M.pde.Burgers(0.01)(u=u, mesh=m), fused=True,
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")]),
+    "apply_ns2d_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(232, (32, 32), 6, 1.0), batch=2, channels=1,
+                           fn=lambda M, u, m: M.pde.NavierStokesVorticity(100)(u=u, mesh=m), fused=True,
+        lin=[(1.0 / 100, ("laplacian",))], nl=[(-1.0, "vorticity_convection")]),
+    "apply_ksnd2d_n32": dict(mesh=[(0, 10 * math.pi, 32)] * 2, ic=_bl(233, (32, 32), 4, 0.5), batch=2, channels=1,
+                             fn=lambda M, u, m: M.pde.KuramotoSivashinskyHighDim()(u=u, mesh=m), fused=True,
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "ks_convection")]),
+    "apply_nsvel2d_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(234, (32, 32), 6, 1.0), batch=1, channels=2,
+                              fn=lambda M, u, m: M.pde.NavierStokes(100)(u=u, mesh=m), fused=True,
+        lin=[(1.0 / 100, ("laplacian",))], nl=[(1.0, "ns_pressure_convection")]),
+    "apply_kdv1d_n64": dict(mesh=[(0, 20.0, 64)], ic=_bl(235, (64,), 5, 1.0), batch=2, channels=1,
+                            fn=lambda M, u, m: M.pde.KortewegDeVries()(u=u, mesh=m), fused=True,
+        lin=[(-1.0, ("spatial_derivative", 0, 3))], nl=[(6.0, "convection")]),
+    "apply_burgers3d_n16": dict(mesh=[(0, TWO_PI, 16)] * 3, ic=_bl(236, (16, 16, 16), 3, 1.0), batch=1, channels=3,
+                                fn=lambda M, u, m: M.pde.Burgers(0.005)(u=u, mesh=m), fused=True,
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")]),
+    "apply_heat2d_n32": dict(mesh=[(0, 1, 32)] * 2, ic=_bl(237, (32, 32), 5, 1.0), batch=2, channels=1,
+                             fn=lambda M, u, m: (0.05 * M.operator.Laplacian())(u=u, mesh=m), fused=True,
+        lin=[(0.05, ("laplacian",))], nl=[]),
+    "apply_grad_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(238, (32, 32), 6, 1.0), batch=2, channels=1,
+                           fn=lambda M, u, m: M.functional.grad(u, mesh=m)),
+    "apply_div_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(239, (32, 32), 6, 1.0), batch=2, channels=2,
+                          fn=lambda M, u, m: M.functional.div(u, mesh=m)),
+    "apply_curl2d_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(240, (32, 32), 6, 1.0), batch=2, channels=2,
+                             fn=lambda M, u, m: M.functional.curl(u, mesh=m)),
+    "apply_curl3d_n16": dict(mesh=[(0, TWO_PI, 16)] * 3, ic=_bl(241, (16, 16, 16), 3, 1.0), batch=1, channels=3,
+                             fn=lambda M, u, m: M.functional.curl(u, mesh=m)),
+    "apply_vort2vel_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(242, (32, 32), 6, 1.0), batch=2, channels=1,
+                               fn=lambda M, u, m: M.functional.vorticity2velocity(u, mesh=m)),
+    "apply_vort2press_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(243, (32, 32), 6, 1.0), batch=2, channels=1,
+                                 fn=lambda M, u, m: M.functional.vorticity2pressure(u, mesh=m)),
+    "apply_vel2press_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(244, (32, 32), 6, 1.0), batch=2, channels=2,
+                                fn=lambda M, u, m: M.functional.velocity2pressure(u, mesh=m)),
+    "apply_vort2press_op_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(245, (32, 32), 6, 1.0), batch=2, channels=1,
+                                    fn=lambda M, u, m: M.operator.Vorticity2Pressure()(u=u, mesh=m)),
+    "apply_vel2press_op_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(246, (32, 32), 6, 1.0), batch=2, channels=2,
+                                   fn=lambda M, u, m: M.operator.Velocity2Pressure()(u=u, mesh=m)),
+    "apply_laplacian_fn_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(247, (32, 32), 6, 1.0), batch=2, channels=1,
+                                   fn=lambda M, u, m: M.functional.laplacian(u, mesh=m), fused=True,
+        lin=[(1.0, ("laplacian",))], nl=[]),
+    "apply_convection_fn_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(248, (32, 32), 6, 1.0), batch=2, channels=2,
+                                    fn=lambda M, u, m: M.functional.convection(u, mesh=m), fused=True,
+        lin=[], nl=[(1.0, "convection")]),
+    "apply_solve_biharmonic_n32": dict(mesh=[(0, TWO_PI, 32)] * 2, ic=_bl(249, (32, 32), 6, 1.0), batch=2, channels=1,
+                                       fn=lambda M, u, m: M.operator.Biharmonic().solve(u, mesh=m, n_channel=1)),
+}
+
+
+def apply_input(name: str) -> np.ndarray:
+    c = APPLY_CASES[name]
     return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)

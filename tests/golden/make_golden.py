@@ -82,6 +82,15 @@ def main(ref_root: str) -> None:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
         print(name, payload["final"].shape, payload["integrator"])
 
+    # One-shot evaluation (Operator.__call__, solve, functional.*) in float64.
+    for name, case in C.APPLY_CASES.items():
+        if only and name not in only:
+            continue
+        u = torch.tensor(C.apply_input(name), dtype=torch.float64)
+        out = case["fn"](M, u, case["mesh"])
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), out=out.numpy())
+        print(name, tuple(out.shape))
+
     # Gradients by the reference's own autograd (float64): d loss / d u0, d loss / d nu.
     for name, case in C.GRAD_CASES.items():
         if only and name not in only:

@@ -70,3 +70,10 @@ def test_masks_match_reference():
         rate = {"0.6667": 2.0 / 3.0, "0.5000": 0.5, "1.0000": 1.0}[key.split("_r")[-1]]
         m = S.OMesh([(0, 2 * np.pi, n)], dtype).low_pass_filter(rate).reshape(-1)
         np.testing.assert_array_equal(m, g[key], err_msg=key)
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in C.APPLY_CASES.items() if "lin" in c))
+def test_oracle_one_shot_evaluation_matches_reference(name):
+    case = C.APPLY_CASES[name]
+    out = S.apply_operator(C.apply_input(name), case["mesh"], case["lin"], case["nl"])
+    assert S.rel_l2(out, _load(name)["out"]) < 1e-10

@@ -6,7 +6,7 @@ trajectory recorders) and runs the time stepping in hand-written sm_103a
 CUDA kernels behind a C ABI (include/torchfsm_gb300.h).
 """
 
-from . import integrator, mesh, operator, pde, traj_recorder, utils
+from . import functional, integrator, mesh, operator, pde, traj_recorder, utils
 from .mesh import FourierMesh, MeshGrid
 from .operator import Operator
 

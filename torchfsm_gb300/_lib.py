@@ -49,6 +49,7 @@ FSM_RK4_38RULE = 27
 FSM_RK_DORPI45 = 28
 FSM_RK_FEHLBERG45 = 29
 FSM_RK_CASHKARP45 = 30
+FSM_APPLY = 40
 
 # Every symbol the header declares; tests check that the library exports them.
 EXPORTS = (

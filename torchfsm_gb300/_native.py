@@ -67,6 +67,10 @@ def lower(linear_terms, nonlinear_terms, f_mesh, n_channel: int, de_aliasing_rat
     from .operator.generic._convection import _ConvectionCore
 
     prog = SpectralProgram(tuple(tuple(m) for m in f_mesh.mesh_info), n_channel)
+    for _, fun in linear_terms:
+        sym = fun(f_mesh, n_channel)
+        if isinstance(sym, torch.Tensor) and sym.dim() >= 2 and sym.shape[1] not in (1, n_channel):
+            raise _lib.UnsupportedProgram(_lib.FSM_ERR_UNSUPPORTED, "a linear term that changes the channel count")
     prog.linear_terms = list(linear_terms)
     kinds = {}
     for coef, fun in nonlinear_terms:

@@ -86,6 +86,10 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
   const int64_t idx = first + k;
   const cd l = L ? mk(L[idx % lcount].x, L[idx % lcount].y) : mk(0.0, 0.0);
   const cd hl = dt * l;
+  if (integ == FSM_APPLY) {
+    tab[idx] = tof(l);
+    return;
+  }
   if (is_rk(integ)) {
     // explicit Runge-Kutta slopes dt (L a + N): the tables are dt L and dt
     tab[idx] = tof(hl);

@@ -80,6 +80,7 @@ static __constant__ RKTableau kRKTab[10] = {
 
 __host__ __device__ inline int scheme_stages(int integ) {
   if (is_rk(integ)) return rk_tableau(integ).s;
+  if (integ == FSM_APPLY) return 1;
   switch (integ) {
     case FSM_SETDRK4: return 4;
     case FSM_SETDRK3: return 3;
@@ -99,6 +100,7 @@ __host__ __device__ inline int scheme_stages(int integ) {
 //  ETDRK0: E
 __host__ __device__ inline int scheme_tables(int integ) {
   if (is_rk(integ)) return 2;  // dt L, dt
+  if (integ == FSM_APPLY) return 1;  // L
   switch (integ) {
     case FSM_SETDRK4: return 6;
     case FSM_SETDRK3: return 7;
@@ -255,6 +257,11 @@ __device__ __forceinline__ float2 etd_stage(int integ, int s, float2 nv, float2*
                                             float2* __restrict__ acc, float2* __restrict__ q,
                                             const float2* __restrict__ tab, int64_t ts, int64_t astride = 0) {
   if (is_rk(integ)) return rk_stage(integ, s, nv, u, acc, astride, tab, ts);
+  if (integ == FSM_APPLY) {  // the right-hand side L u + N(u) replaces the state
+    const float2 r = cfma(tab[0], *u, nv);
+    *u = r;
+    return r;
+  }
   switch (integ) {
     case FSM_SETDRK4:
       switch (s) {

@@ -11,5 +11,7 @@ from ._base import (
     OperatorLike,
     check_value_with_mesh,
 )
-from .dedicated import KSConvection, NSPressureConvection, VorticityConvection
-from .generic import Biharmonic, ConservativeConvection, Convection, ImplicitSource, Laplacian, SpatialDerivative
+from .dedicated import (KSConvection, NSPressureConvection, Velocity2Pressure, Vorticity2Pressure, Vorticity2Velocity,
+                        VorticityConvection)
+from .generic import (Biharmonic, ConservativeConvection, Convection, Curl, Div, Grad, ImplicitSource, Laplacian,
+                      SpatialDerivative)

@@ -125,7 +125,9 @@ class _InverseSolveMixin:
         if not (mesh is None and n_channel is None):
             mesh = self._state_dict["f_mesh"] if mesh is None else mesh
             n_channel = self._state_dict["n_channel"] if n_channel is None else n_channel
-            self.register_mesh(mesh, n_channel)
+            src = b if b is not None else b_fft
+            # a mesh given as a list is registered on the right-hand side's device
+            self.register_mesh(mesh, n_channel, device=None if isinstance(mesh, FourierMesh) else src.device)
         if self._state_dict["invert_linear_coef"] is None:
             lin = self.linear_coef
             self._state_dict["invert_linear_coef"] = torch.where(lin == 0, 1.0, 1 / lin)
@@ -193,6 +195,7 @@ class OperatorLike(_MutableMixIn):
             "operator": None,
             "integrator": None,
             "invert_linear_coef": None,
+            "apply_plan": None,  # library plan of the one-shot evaluation (FSM_APPLY), False if not lowerable
         }
         self._linear_terms = []
         self._nonlinear_funcs = []
@@ -449,12 +452,25 @@ class OperatorLike(_MutableMixIn):
 
     def __call__(self, u: Optional[Tensor] = None, u_fft: Optional[Tensor] = None, mesh: Optional[MeshLike] = None,
                  return_in_fourier: bool = False) -> Tensor:
-        """L u_hat + N(u_hat) once (operator/_base.py:753-790)."""
+        """L u_hat + N(u_hat) once (operator/_base.py:753-790).
+
+        Programs the library lowers (the ones ``integrate`` runs fused) evaluate through the
+        fused kernels: a one-step launch sequence of the FSM_APPLY scheme writes the
+        right-hand side over a half-spectrum copy of the (real) input. Other programs
+        (channel-changing post-processing cores, Python callables) evaluate their cores with
+        torch on the input's device."""
         if self._state_dict["f_mesh"] is None or mesh is not None:
             mesh, n_channel = self._pre_check(u, u_fft, mesh)
             self.register_mesh(mesh, n_channel)
         else:
             self._pre_check(u=u, u_fft=u_fft, mesh=self._state_dict["f_mesh"])
+        fused = self._apply_fused(u, u_fft)
+        if fused is not None:
+            half, sp, dtype = fused
+            if return_in_fourier:
+                out = sp.half_to_full(half)
+                return out.to(torch.complex128) if dtype == torch.float64 else out
+            return sp.to_physical(half, keep_input=False).to(dtype)
         if self._state_dict["operator"] is None:
             self._build_operator()
         f_mesh = self._state_dict["f_mesh"]
@@ -462,6 +478,38 @@ class OperatorLike(_MutableMixIn):
             u_fft = f_mesh.fft(u)
         value_fft = self._state_dict["operator"](u_fft)
         return value_fft if return_in_fourier else f_mesh.ifft(value_fft).real
+
+    @torch.no_grad()
+    def _apply_fused(self, u: Optional[Tensor], u_fft: Optional[Tensor]):
+        """(half spectrum of L u + N(u), its Spectral, the input's real dtype) through the library,
+        or None where the program does not lower or the input is not on a CUDA device."""
+        src = u if u is not None else u_fft
+        if src is None or not src.is_cuda or self._state_dict["apply_plan"] is False:
+            return None
+        if any(isinstance(c, Tensor) and c.requires_grad for c, _ in self._linear_terms):
+            return None  # keep autograd through torch for tensor coefficients that want gradients
+        plan = self._state_dict["apply_plan"]
+        if plan is None or plan.device != src.device:
+            f_mesh = self._state_dict["f_mesh"]
+            try:
+                prog = _native.lower(self._linear_terms, self._nonlinear_funcs, f_mesh,
+                                     self._state_dict["n_channel"], self._de_aliasing_rate)
+                plan = _native.NativePlan(prog, 1.0, _lib.FSM_APPLY, src.device,
+                                          linear_coef64=self._linear_coef64(src.device))
+            except _lib.UnsupportedProgram:
+                self._state_dict["apply_plan"] = False
+                return None
+            self._state_dict["apply_plan"] = plan
+        sp = _native.Spectral(plan)
+        if u is not None:
+            dtype = u.dtype
+            half = sp.to_half(u)
+        else:
+            dtype = torch.float64 if u_fft.dtype == torch.complex128 else torch.float32
+            half = sp.full_to_half(u_fft)
+        half = half.contiguous()
+        plan.integrate_half(half, 1)
+        return half, sp, dtype
 
     def to(self, device=None, dtype=None):
         if self._state_dict["f_mesh"] is not None:

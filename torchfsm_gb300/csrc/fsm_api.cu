@@ -577,6 +577,90 @@ size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps)
 
 namespace {
 
+// Batches at or above this many spectral points run as two halves on two streams.
+constexpr int64_t kSplitPoints = (int64_t)3 << 19;
+
+// Two non-blocking streams per (device, caller stream), created once, with the caller's
+// priority, for the two halves of a split batch.
+static std::mutex g_split_mutex;
+static std::map<std::pair<int, cudaStream_t>, std::pair<cudaStream_t, cudaStream_t>> g_split;
+
+int split_streams(cudaStream_t st, cudaStream_t out[2]) {
+  int dev = 0;
+  int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_split_mutex);
+  auto it = g_split.find({dev, st});
+  if (it == g_split.end()) {
+    int prio = 0;
+    if ((rc = cuda_check(cudaStreamGetPriority(st, &prio), "cudaStreamGetPriority"))) return rc;
+    cudaStream_t s0, s1;
+    if ((rc = cuda_check(cudaStreamCreateWithPriority(&s0, cudaStreamNonBlocking, prio), "stream"))) return rc;
+    if ((rc = cuda_check(cudaStreamCreateWithPriority(&s1, cudaStreamNonBlocking, prio), "stream"))) return rc;
+    it = g_split.emplace(std::make_pair(dev, st), std::make_pair(s0, s1)).first;
+  }
+  out[0] = it->second.first;
+  out[1] = it->second.second;
+  return FSM_OK;
+}
+
+// The arguments of samples [b0, b0 + n) of a batch: state, trajectory, per-sample tables and
+// sources offset to the first sample, the pass arrays laid out for n samples in their own
+// slice of the workspace (the workspace holds the arrays of all samples, sample-major slices).
+StepArgs batch_arrays(const FsmPlan* p, StepArgs a, float2* arr, int b0, int n) {
+  const int64_t S = p->S;
+  const int64_t per_sample = (int64_t)(p->n_aux * p->C + p->n_mid + p->n_mid2 + p->n_prod) * S;
+  a.state += (int64_t)b0 * p->C * S;
+  if (a.traj) a.traj += (int64_t)b0 * a.n_frames * p->C * S;
+  if (p->lin_batch > 1) a.tab += (int64_t)b0 * p->lin_ch * S;
+  if (a.src && p->src_batch > 1) a.src += (int64_t)b0 * p->C * S;
+  a.aux = arr + (int64_t)b0 * per_sample;
+  a.mid = a.aux + (int64_t)n * p->n_aux * p->C * S;
+  a.mid2 = a.mid + (int64_t)n * p->n_mid * S;
+  a.prod = a.mid2 + (int64_t)n * p->n_mid2 * S;
+  a.B = n;
+  return a;
+}
+
+// The launch sequence of the plane (2D) / volume (3D) passes, step by step: prime() before
+// the first step, then step(k) for k = 0 .. steps-1, on one stream.
+struct PlaneSequence {
+  const FsmPlan* p;
+  StepArgs a;
+  const int32_t* record_slot;
+  int32_t steps;
+  cudaStream_t st;
+  LaunchProfile* prof;
+
+  int prime() {
+    a.stage = -1;
+    a.emit = steps > 0;
+    a.slot = record_slot ? record_slot[0] : -1;
+    return timed(prof, kProfPrime, [&] { return launch_plane_col(p, a, st); });
+  }
+  int step(int k) {
+    int rc;
+    const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
+    const bool vol = p->path == 4;
+    for (int s = 0; s < p->nstages; ++s) {
+      if (vol) {
+        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_inv(p, a, st); }))) return rc;
+        if ((rc = timed(prof, kProfRow, [&] { return launch_volume_axis2(p, a, st); }))) return rc;
+        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_fwd(p, a, st); }))) return rc;
+      } else {
+        if ((rc = timed(prof, kProfRow, [&] { return launch_plane_row(p, a, st); }))) return rc;
+      }
+      if (ks_mean && (rc = timed(prof, kProfOther, [&] { return launch_ks_mean(p, a, st); }))) return rc;
+      const bool last = s == p->nstages - 1;
+      a.stage = s;
+      a.emit = !(last && k == steps - 1);
+      a.slot = (last && record_slot) ? record_slot[k + 1] : -1;
+      if ((rc = timed(prof, kProfColumn, [&] { return launch_plane_col(p, a, st); }))) return rc;
+    }
+    return FSM_OK;
+  }
+};
+
 int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
                    int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof) {
   if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
@@ -648,37 +732,55 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
 
   // plane (2D) / volume (3D) passes
   float2* arr = (float2*)(ws + off_arrays);
-  const int64_t per_field = p->S;
-  a.aux = arr;
-  a.mid = a.aux + (int64_t)batch * p->n_aux * p->C * per_field;
-  a.mid2 = a.mid + (int64_t)batch * p->n_mid * per_field;
-  a.prod = a.mid2 + (int64_t)batch * p->n_mid2 * per_field;
   a.slots = nullptr;
   const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
-  const bool vol = p->path == 4;
-  a.stage = -1;
-  a.emit = steps > 0;
-  a.slot = record_slot ? record_slot[0] : -1;
-  if ((rc = timed(prof, kProfPrime, [&] { return launch_plane_col(p, a, st); }))) return rc;
-  for (int step = 0; step < steps; ++step) {
-    for (int s = 0; s < p->nstages; ++s) {
-      if (vol) {
-        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_inv(p, a, st); }))) return rc;
-        if ((rc = timed(prof, kProfRow, [&] { return launch_volume_axis2(p, a, st); }))) return rc;
-        if ((rc = timed(prof, kProfOther, [&] { return launch_volume_axis1_fwd(p, a, st); }))) return rc;
-      } else {
-        if ((rc = timed(prof, kProfRow, [&] { return launch_plane_row(p, a, st); }))) return rc;
-      }
-      if (ks_mean && (rc = timed(prof, kProfOther, [&] { return launch_ks_mean(p, a, st); }))) return rc;
-      const bool last = s == p->nstages - 1;
-      a.stage = s;
-      a.emit = !(last && step == steps - 1);
-      a.slot = (last && record_slot) ? record_slot[step + 1] : -1;
-      if ((rc = timed(prof, kProfColumn, [&] { return launch_plane_col(p, a, st); }))) return rc;
-    }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if ((rc = cuda_check(cudaStreamIsCapturing(st, &cap), "stream capture query"))) return rc;
+  // Large batches run as two halves on two streams forked from the caller's: the halves'
+  // launches interleave on the device (the column passes of one overlap the row passes of
+  // the other), which fills the SMs better than one launch sequence of twice the size.
+  // Samples are independent except under the KS batch-wide mean; capture and the profiled
+  // (per-launch timed) call keep one sequence.
+  const bool split = !prof && !ks_mean && cap == cudaStreamCaptureStatusNone && batch >= 2 &&
+                     (int64_t)batch * p->S >= kSplitPoints;
+  if (!split) {
+    PlaneSequence q{p, batch_arrays(p, a, arr, 0, batch), record_slot, steps, st, prof};
+    if ((rc = q.prime())) return rc;
+    for (int k = 0; k < steps; ++k)
+      if ((rc = q.step(k))) return rc;
+    return FSM_OK;
   }
-  return FSM_OK;
+  // The halves are enqueued step by step, each step of one half waiting for the previous
+  // step of the other, so that neither runs ahead and leaves the other alone at the end.
+  cudaStream_t sub[2];
+  if ((rc = split_streams(st, sub))) return rc;
+  cudaEvent_t fork, done[2];
+  if ((rc = cuda_check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event"))) return rc;
+  for (int h = 0; h < 2; ++h)
+    if ((rc = cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "event"))) return rc;
+  const int half = batch / 2;
+  PlaneSequence q[2] = {{p, batch_arrays(p, a, arr, 0, half), record_slot, steps, sub[0], nullptr},
+                        {p, batch_arrays(p, a, arr, half, batch - half), record_slot, steps, sub[1], nullptr}};
+  rc = cuda_check(cudaEventRecord(fork, st), "fork");
+  for (int h = 0; h < 2 && !rc; ++h) {
+    rc = cuda_check(cudaStreamWaitEvent(sub[h], fork, 0), "fork wait");
+    if (!rc) rc = q[h].prime();
+    if (!rc) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
+  }
+  for (int k = 0; k < steps && !rc; ++k) {
+    for (int h = 0; h < 2 && !rc; ++h) {
+      rc = cuda_check(cudaStreamWaitEvent(sub[h], done[1 - h], 0), "step wait");
+      if (!rc) rc = q[h].step(k);
+    }
+    for (int h = 0; h < 2 && !rc; ++h) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
+  }
+  for (int h = 0; h < 2 && !rc; ++h) rc = cuda_check(cudaStreamWaitEvent(st, done[h], 0), "join wait");
+  cudaEventDestroy(fork);  // released once the recorded work completes
+  cudaEventDestroy(done[0]);
+  cudaEventDestroy(done[1]);
+  return rc;
 }
+
 
 }  // namespace
 

@@ -577,15 +577,19 @@ size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps)
 
 namespace {
 
-// Batches at or above this many spectral points run as two halves on two streams.
+// Batches at or above kSplitPoints spectral points run in parts of about kPartPoints points
+// (2 to kMaxParts parts, at most one per sample) on as many streams. Measured on 256^2 x 64
+// (2.1 M points): one sequence 322 us per step, 2 parts 284, 4 parts 270, 8 parts 261.
 constexpr int64_t kSplitPoints = (int64_t)3 << 19;
+constexpr int64_t kPartPoints = (int64_t)1 << 18;
+constexpr int kMaxParts = 8;
 
-// Two non-blocking streams per (device, caller stream), created once, with the caller's
-// priority, for the two halves of a split batch.
+// kMaxParts non-blocking streams per (device, caller stream), created once, with the
+// caller's priority, for the parts of a split batch.
 static std::mutex g_split_mutex;
-static std::map<std::pair<int, cudaStream_t>, std::pair<cudaStream_t, cudaStream_t>> g_split;
+static std::map<std::pair<int, cudaStream_t>, std::vector<cudaStream_t>> g_split;
 
-int split_streams(cudaStream_t st, cudaStream_t out[2]) {
+int split_streams(cudaStream_t st, cudaStream_t* out) {
   int dev = 0;
   int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   if (rc) return rc;
@@ -594,13 +598,12 @@ int split_streams(cudaStream_t st, cudaStream_t out[2]) {
   if (it == g_split.end()) {
     int prio = 0;
     if ((rc = cuda_check(cudaStreamGetPriority(st, &prio), "cudaStreamGetPriority"))) return rc;
-    cudaStream_t s0, s1;
-    if ((rc = cuda_check(cudaStreamCreateWithPriority(&s0, cudaStreamNonBlocking, prio), "stream"))) return rc;
-    if ((rc = cuda_check(cudaStreamCreateWithPriority(&s1, cudaStreamNonBlocking, prio), "stream"))) return rc;
-    it = g_split.emplace(std::make_pair(dev, st), std::make_pair(s0, s1)).first;
+    std::vector<cudaStream_t> v(kMaxParts);
+    for (auto& sv : v)
+      if ((rc = cuda_check(cudaStreamCreateWithPriority(&sv, cudaStreamNonBlocking, prio), "stream"))) return rc;
+    it = g_split.emplace(std::make_pair(dev, st), v).first;
   }
-  out[0] = it->second.first;
-  out[1] = it->second.second;
+  for (int h = 0; h < kMaxParts; ++h) out[h] = it->second[h];
   return FSM_OK;
 }
 
@@ -736,9 +739,9 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   if ((rc = cuda_check(cudaStreamIsCapturing(st, &cap), "stream capture query"))) return rc;
-  // Large batches run as two halves on two streams forked from the caller's: the halves'
-  // launches interleave on the device (the column passes of one overlap the row passes of
-  // the other), which fills the SMs better than one launch sequence of twice the size.
+  // Large batches run in parts on streams forked from the caller's: the parts' launches
+  // interleave on the device (the column passes of one overlap the row passes of another),
+  // which fills the SMs better than one launch sequence of the whole batch.
   // Samples are independent except under the KS batch-wide mean; capture and the profiled
   // (per-launch timed) call keep one sequence.
   const bool split = !prof && !ks_mean && cap == cudaStreamCaptureStatusNone && batch >= 2 &&
@@ -750,34 +753,38 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
       if ((rc = q.step(k))) return rc;
     return FSM_OK;
   }
-  // The halves are enqueued step by step, each step of one half waiting for the previous
-  // step of the other, so that neither runs ahead and leaves the other alone at the end.
-  cudaStream_t sub[2];
+  // The parts are enqueued step by step, each part's step waiting for the previous step of
+  // the part before it (a ring), so that none runs ahead and leaves the others alone at the end.
+  int64_t parts = (int64_t)batch * p->S / kPartPoints;
+  parts = parts < 2 ? 2 : (parts > kMaxParts ? kMaxParts : parts);
+  const int NP = (int)(parts < batch ? parts : batch);
+  cudaStream_t sub[kMaxParts];
   if ((rc = split_streams(st, sub))) return rc;
-  cudaEvent_t fork, done[2];
+  cudaEvent_t fork, done[kMaxParts];
   if ((rc = cuda_check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event"))) return rc;
-  for (int h = 0; h < 2; ++h)
+  for (int h = 0; h < NP; ++h)
     if ((rc = cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "event"))) return rc;
-  const int half = batch / 2;
-  PlaneSequence q[2] = {{p, batch_arrays(p, a, arr, 0, half), record_slot, steps, sub[0], nullptr},
-                        {p, batch_arrays(p, a, arr, half, batch - half), record_slot, steps, sub[1], nullptr}};
+  PlaneSequence q[kMaxParts];
+  for (int h = 0; h < NP; ++h) {
+    const int b0 = (int)((int64_t)batch * h / NP), b1 = (int)((int64_t)batch * (h + 1) / NP);
+    q[h] = PlaneSequence{p, batch_arrays(p, a, arr, b0, b1 - b0), record_slot, steps, sub[h], nullptr};
+  }
   rc = cuda_check(cudaEventRecord(fork, st), "fork");
-  for (int h = 0; h < 2 && !rc; ++h) {
+  for (int h = 0; h < NP && !rc; ++h) {
     rc = cuda_check(cudaStreamWaitEvent(sub[h], fork, 0), "fork wait");
     if (!rc) rc = q[h].prime();
     if (!rc) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
   }
   for (int k = 0; k < steps && !rc; ++k) {
-    for (int h = 0; h < 2 && !rc; ++h) {
-      rc = cuda_check(cudaStreamWaitEvent(sub[h], done[1 - h], 0), "step wait");
+    for (int h = 0; h < NP && !rc; ++h) {
+      rc = cuda_check(cudaStreamWaitEvent(sub[h], done[(h + NP - 1) % NP], 0), "step wait");
       if (!rc) rc = q[h].step(k);
     }
-    for (int h = 0; h < 2 && !rc; ++h) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
+    for (int h = 0; h < NP && !rc; ++h) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
   }
-  for (int h = 0; h < 2 && !rc; ++h) rc = cuda_check(cudaStreamWaitEvent(st, done[h], 0), "join wait");
+  for (int h = 0; h < NP && !rc; ++h) rc = cuda_check(cudaStreamWaitEvent(st, done[h], 0), "join wait");
   cudaEventDestroy(fork);  // released once the recorded work completes
-  cudaEventDestroy(done[0]);
-  cudaEventDestroy(done[1]);
+  for (int h = 0; h < NP; ++h) cudaEventDestroy(done[h]);
   return rc;
 }
 

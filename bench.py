@@ -181,7 +181,7 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
     state = state0.clone()
     ws = torch.empty(plan.workspace_bytes(B, TIME_STEPS), dtype=torch.uint8, device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
-    launches_per_step = plan.launch_count(TIME_STEPS)
+    launches_per_step = plan.launch_count(TIME_STEPS, B)
 
     def step():
         state.copy_(state0)
@@ -531,7 +531,7 @@ def run_burgers3d(args):
             "data": "synthetic (seeded GRF velocity)",
             "config": {"workload": "burgers3d_256cubed_200steps", "result_finite": finite,
                        "l2": "inputs (200 MB state, 1.6 GB workspace) larger than L2"},
-            "gpu_launches": plan.launch_count(steps) * args.steps,
+            "gpu_launches": plan.launch_count(steps, 1) * args.steps,
             "roofline": {"bound": "hbm", "per_kernel_ms": {k: v["avg_ms"] for k, v in prof.items() if v["launches"]},
                          "step_model_bytes_per_dof_step": 276,
                          "step_achieved_gbs": 276.0 * dof_steps / (ms * 1e-3) / 1e9, "peak": _peaks()[0]},

@@ -149,8 +149,10 @@ int fsm_plan_destroy(FsmPlan* plan);
 /* Bytes of device workspace fsm_integrate needs for `batch` samples and `steps` steps. */
 int fsm_plan_workspace_bytes(const FsmPlan* plan, int32_t batch, int32_t steps, size_t* bytes);
 
-/* Number of kernel launches fsm_integrate makes for `steps` steps. */
-int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches);
+/* Number of kernel launches fsm_integrate makes for `batch` samples and `steps` steps outside
+ * stream capture (large batches run in parts, each with its own launches); batch 0 counts
+ * one launch sequence (what a captured call makes). */
+int fsm_plan_launch_count(const FsmPlan* plan, int32_t batch, int32_t steps, int64_t* launches);
 
 /* Advance `state` (half spectra, [batch][C][S] complex64, in place) by `steps`
  * steps of dt. record_slot (HOST, steps+1 entries, or NULL): for step i

@@ -135,7 +135,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_plan_move_batch.argtypes = [vp, i32, i32, vp]
         lib.fsm_plan_tables.argtypes = [vp, vp, sz, ctypes.POINTER(i32), ctypes.POINTER(i64), vp]
         lib.fsm_plan_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
-        lib.fsm_plan_launch_count.argtypes = [vp, i32, ctypes.POINTER(i64)]
+        lib.fsm_plan_launch_count.argtypes = [vp, i32, i32, ctypes.POINTER(i64)]
         lib.fsm_integrate.argtypes = [vp, i32, vp, i32, vp, vp, i32, vp, sz, vp]
         lib.fsm_integrate_profiled.argtypes = [vp, i32, vp, i32, vp, sz, vp, ctypes.POINTER(ctypes.c_double),
                                                ctypes.POINTER(i64)]

@@ -278,9 +278,9 @@ class NativePlan:
         _lib.check(_lib.load().fsm_plan_workspace_bytes(self.handle, batch, steps, ctypes.byref(out)))
         return int(out.value)
 
-    def launch_count(self, steps: int) -> int:
+    def launch_count(self, steps: int, batch: int = 0) -> int:
         out = ctypes.c_int64()
-        _lib.check(_lib.load().fsm_plan_launch_count(self.handle, steps, ctypes.byref(out)))
+        _lib.check(_lib.load().fsm_plan_launch_count(self.handle, batch, steps, ctypes.byref(out)))
         return int(out.value)
 
     def integrate_half(self, state: torch.Tensor, steps: int, slots: Optional[Sequence[int]] = None,

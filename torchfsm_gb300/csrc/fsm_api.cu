@@ -502,12 +502,12 @@ int fsm_plan_workspace_bytes(const FsmPlan* plan, int32_t batch, int32_t steps, 
   return FSM_OK;
 }
 
-int fsm_plan_launch_count(const FsmPlan* plan, int32_t steps, int64_t* launches) {
-  if (!plan || !launches || steps < 0) return set_error(FSM_ERR_INVALID, "launch_count arguments");
+int fsm_plan_launch_count(const FsmPlan* plan, int32_t batch, int32_t steps, int64_t* launches) {
+  if (!plan || !launches || steps < 0 || batch < 0) return set_error(FSM_ERR_INVALID, "launch_count arguments");
   if (plan->path == 2 || plan->path == 4) {
     const int64_t per_stage = (plan->path == 4 ? 4 : 2) +
                               ((plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) ? 1 : 0);
-    *launches = 1 + (int64_t)steps * plan->nstages * per_stage;
+    *launches = (int64_t)fsm::split_parts(plan, batch) * (1 + (int64_t)steps * plan->nstages * per_stage);
   } else if (plan->path == 1 && plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN)) {
     *launches = steps > 0 ? 3 : 1;  // line kernel, batch means of k = 0, k = 0 fix-up
   } else {
@@ -575,14 +575,27 @@ size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps)
 }
 }  // namespace fsm
 
-namespace {
-
+namespace fsm {
 // Batches at or above kSplitPoints spectral points run in parts of about kPartPoints points
 // (2 to kMaxParts parts, at most one per sample) on as many streams. Measured on 256^2 x 64
 // (2.1 M points): one sequence 322 us per step, 2 parts 284, 4 parts 270, 8 parts 261.
 constexpr int64_t kSplitPoints = (int64_t)3 << 19;
 constexpr int64_t kPartPoints = (int64_t)1 << 18;
 constexpr int kMaxParts = 8;
+
+// Number of parts an uncaptured, unprofiled integrate of `batch` samples runs in (1: one sequence).
+int split_parts(const FsmPlan* p, int batch) {
+  if (p->path != 2 && p->path != 4) return 1;
+  if (p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN)) return 1;  // the batch mean couples the samples
+  if (batch < 2 || (int64_t)batch * p->S < kSplitPoints) return 1;
+  int64_t parts = (int64_t)batch * p->S / kPartPoints;
+  parts = parts < 2 ? 2 : (parts > kMaxParts ? kMaxParts : parts);
+  return (int)(parts < batch ? parts : batch);
+}
+}  // namespace fsm
+
+namespace {
+using fsm::kMaxParts;
 
 // kMaxParts non-blocking streams per (device, caller stream), created once, with the
 // caller's priority, for the parts of a split batch.
@@ -744,8 +757,8 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   // which fills the SMs better than one launch sequence of the whole batch.
   // Samples are independent except under the KS batch-wide mean; capture and the profiled
   // (per-launch timed) call keep one sequence.
-  const bool split = !prof && !ks_mean && cap == cudaStreamCaptureStatusNone && batch >= 2 &&
-                     (int64_t)batch * p->S >= kSplitPoints;
+  const int NP = (prof || cap != cudaStreamCaptureStatusNone) ? 1 : fsm::split_parts(p, batch);
+  const bool split = NP > 1;
   if (!split) {
     PlaneSequence q{p, batch_arrays(p, a, arr, 0, batch), record_slot, steps, st, prof};
     if ((rc = q.prime())) return rc;
@@ -755,9 +768,6 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   }
   // The parts are enqueued step by step, each part's step waiting for the previous step of
   // the part before it (a ring), so that none runs ahead and leaves the others alone at the end.
-  int64_t parts = (int64_t)batch * p->S / kPartPoints;
-  parts = parts < 2 ? 2 : (parts > kMaxParts ? kMaxParts : parts);
-  const int NP = (int)(parts < batch ? parts : batch);
   cudaStream_t sub[kMaxParts];
   if ((rc = split_streams(st, sub))) return rc;
   cudaEvent_t fork, done[kMaxParts];

@@ -70,6 +70,8 @@ int launch_plane_col(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_row(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_ks_mean(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_pointwise(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+// Parts (streams) an uncaptured integrate of `batch` samples is split into; 1: one sequence.
+int split_parts(const FsmPlan* p, int batch);
 
 // Raise a kernel's dynamic shared-memory limit when it needs more than 48 KB. The
 // attribute is per function and per device; the size set is remembered per

@@ -146,7 +146,9 @@ class _Bucket:
             self._advance(self.n_active, k)
             e1 = torch.cuda.Event(enable_timing=True)
             e1.record(self.stream)
-        self.launches += self.plan.launch_count(k)
+        # a captured tick (graph replay) runs one launch sequence; a direct one may run in parts
+        graphed = self.use_graphs and k <= GRAPH_MAX_STEPS and (self.n_active, k) in self.graphs
+        self.launches += self.plan.launch_count(k, 0 if graphed else self.n_active)
         self.tick = (e0, e1, k, self.n_active)
 
     def _advance(self, n: int, k: int) -> None:

@@ -382,6 +382,12 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       if (prog->keep[i]) keep[p->koff[i] + j] = prog->keep[i][j] ? 1 : 0;
     }
   }
+  {
+    // the trailing run of dealiased entries of the last axis' half spectrum
+    const int last = nd - 1, h = mesh->n[last] / 2 + 1;
+    p->ycut = h;
+    while (p->ycut > 0 && keep[p->koff[last] + p->ycut - 1] == 0) --p->ycut;
+  }
   std::vector<float2> tw(kTwiddleMax);
   for (int k = 0; k < kTwiddleMax; ++k) {
     const double ang = 2.0 * M_PI * (double)k / (double)kTwiddleMax;
@@ -725,6 +731,8 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.keepx = p->keep + p->koff[0];
   a.keepy = p->keep + p->koff[p->ndim - 1];
   a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
+  a.ycut = p->ycut;
+  a.prune = p->path == 2 ? 1 : 0;
   a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
   a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));

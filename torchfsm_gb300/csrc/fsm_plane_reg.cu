@@ -242,6 +242,23 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
       axis0_update<NX, KIND, DIM, -1, -1>(a, tileA, b, c0, cg, last);
     }
     if (!a.emit) continue;  // uniform: no further barriers in this group
+    if (DIM == 2 && a.prune && c0 >= a.ycut) {
+      // every column of this tile is dealiased: the next-stage fields are zero here, written
+      // directly (coalesced rows of W columns) without the transforms
+      constexpr int NMO = (KIND == FSM_NL_CONVECTION) ? 2 : K::NMG;  // fields of this channel group
+      const int m0 = (KIND == FSM_NL_CONVECTION) ? cg * 2 : 0;
+#pragma unroll 1
+      for (int mf = 0; mf < NMO; ++mf) {
+        float2* dst = a.mid + ((int64_t)b * a.n_mid + m0 + mf) * S;
+#pragma unroll
+        for (int it = 0; it < NX * W / 256; ++it) {
+          const int idx = threadIdx.x + it * 256;
+          const int row = idx / W, cc = idx % W;
+          if (c0 + cc < inner) dst[(int64_t)row * inner + c0 + cc] = make_float2(0.f, 0.f);
+        }
+      }
+      continue;  // uniform across the CTA
+    }
     __syncthreads();
 
     // Next-stage fields: each group transforms its own column into tileB, then the CTA

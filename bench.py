@@ -729,9 +729,10 @@ def reference_autograd_burgers2d(device, u0h, target, mesh, dt, steps) -> dict:
     return res
 
 
-def ncu_case(workload: str = "ns2d"):
+def ncu_case(workload: str = "ns2d", n3d: int = 256):
     """Small profiling runs. ns2d: full batch (inputs larger than L2), 3 SETDRK4 steps, 25 launches
-    after a 9-launch warm-up. burgers3d: 256^3 x 3, 1 warm-up step then 2 steps."""
+    after a 9-launch warm-up. burgers3d: n3d^3 x 3 (256 by default; 128 for captures of several
+    metrics, whose passes save and restore device memory), 1 warm-up step then 2 steps."""
     import torch
 
     import __graft_entry__ as entry
@@ -740,7 +741,7 @@ def ncu_case(workload: str = "ns2d"):
     from torchfsm_gb300 import initial, pde
 
     if workload == "burgers3d":
-        n = 256
+        n = n3d
         device = torch.device("cuda", 0)
         u0 = torch.tensor(initial.gaussian_random_field((n, n, n), 1, 3, initial.velocity_spectrum, SEED)
                           .astype(np.float32), device=device)
@@ -780,9 +781,10 @@ def main():
                          "burgers3d: 3D Burgers 256^3")
     ap.add_argument("--ncu-case", action="store_true",
                     help="small profiling case: one warm-up step, then 3 time steps of the full batch")
+    ap.add_argument("--ncu-n", type=int, default=256, help="grid size of the burgers3d profiling case")
     args = ap.parse_args()
     if args.ncu_case:
-        ncu_case(args.workload)
+        ncu_case(args.workload, args.ncu_n)
         return
     if args.workload == "burgers1d" and args.impl == "fused":
         run_burgers1d(args)

@@ -553,7 +553,7 @@ def run_serving(args):
     device = torch.device("cuda", 0)
     count = args.requests
     reqs = serving.make_stream(count, seed=7, rate_hz=0.0)
-    server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk)
+    server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk, priority=args.priority)
     server.prepare(sorted({(r.kind, r.n) for r in reqs}))
     # warm-up: a few requests through both paths (kernel attributes, plans of the plain path)
     warm = serving.make_stream(8, seed=99, rate_hz=0.0, max_steps=120)
@@ -595,6 +595,7 @@ def run_serving(args):
             "dtype": "f32/c64", "data": "synthetic (seeded band-limited fields)",
             "config": {"workload": f"serving_{count}_requests", "chunk_steps": args.chunk,
                        "host_loop": "thread per bucket" if args.threaded else "single loop",
+                       "high_priority_buckets": args.priority,
                        "cuda_graphs": f"replayed per (slots, steps) shape for ticks of <= {serving.GRAPH_MAX_STEPS} steps",
                        "mix": "KS 1D L=32pi N in {256..4096} | 2D Burgers nu=0.01 N in {64,128,256}; batch 1-32; "
                               "steps 100-2000; dt 0.01-0.1; ICs |k|<=8, RMS 1 (KS) / 0.25 (Burgers)"},
@@ -775,6 +776,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
     ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
     ap.add_argument("--threaded", type=int, default=1, help="serving: one host worker thread per bucket")
+    ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],
+                    help="serving: buckets on the high-priority streams")
     ap.add_argument("--workload", default="ns2d",
                     choices=["ns2d", "burgers1d", "burgers3d", "serving", "burgers2d_grad"],
                     help="ns2d: the headline (2D NS vorticity 256^2 x 64); burgers1d: 1D Burgers N=128 latency; "

@@ -232,9 +232,12 @@ class SolveServer:
     """Admission by HBM budget, per-bucket ticks on separate streams."""
 
     def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
-                 max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True):
+                 max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True, priority: str = "cheap"):
+        """``priority``: which buckets get the high-priority streams, "cheap" (1D and 64^2 grids,
+        whose requests are short) or "costly" (the large 2D grids, whose requests are the long tail)."""
         self.device = device
         self.graphs = graphs
+        self.priority = priority
         self.budget = hbm_budget_bytes
         self.chunk = chunk
         self.max_slots = max_slots
@@ -247,8 +250,8 @@ class SolveServer:
         lo, hi = torch.cuda.Stream.priority_range()
         for kind, n in keys:
             cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
-            # cheap per-step buckets (1D, small 2D grids) get the higher-priority streams
-            prio = hi if (kind == "ks1d" or n <= 64) else lo
+            cheap = kind == "ks1d" or n <= 64
+            prio = hi if cheap == (self.priority == "cheap") else lo
             self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms, self.graphs)
         torch.cuda.synchronize(self.device)
 

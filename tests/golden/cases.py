@@ -52,14 +52,14 @@ def _kolmogorov_source(mesh_info, batch, channels):
 
 
 CASES = {
-    # BASELINE configuration 1 exactly (README example).
-    "burgers1d_cfg1": dict(
+    # The README example exactly: 1D Burgers nu = 0.01, N = 128, u0 = sin(2 pi x) + 0.5, 200 steps.
+    "burgers1d_readme_n128": dict(
         mesh=[(0, 1, 128)], batch=1, channels=1, dt=0.01, step=200, record=1,
         build=lambda M: M.pde.Burgers(0.01),
         lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
         ic=_sin_plus_half,
     ),
-    # 2D vorticity NS, the cfg2 program on a small grid.
+    # 2D vorticity NS, NavierStokesVorticity(1000), on a small grid.
     "ns2d_n32": dict(
         mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=1, dt=0.01, step=50, record=10,
         build=lambda M: M.pde.NavierStokesVorticity(1000),
@@ -189,7 +189,7 @@ CASES.update({
     ),
 })
 
-# Alternative integrators on the cfg1 program (64 points, 50 steps).
+# Alternative integrators on the README 1D Burgers program (64 points, 50 steps).
 for _name in ("setdrk1", "setdrk2", "setdrk3", "etdrk1", "etdrk2"):
     CASES[f"burgers1d_{_name}"] = dict(
         mesh=[(0, 1, 64)], batch=1, channels=1, dt=0.005, step=50, record=0,

@@ -31,7 +31,6 @@ def main(ref_root: str) -> None:
 
     torch.set_num_threads(max(1, os.cpu_count() or 1))
     import torchfsm  # noqa: F401  (the reference)
-    from torchfsm.integrator import ETDRKIntegrator, SETDRKIntegrator
     from torchfsm.mesh import FourierMesh
     from torchfsm.traj_recorder import AutoRecorder
     from torchfsm.integrator._stable_etdrk._uncached import UnCachedSETDRK4, UnCachedSETDRK3
@@ -41,15 +40,6 @@ def main(ref_root: str) -> None:
     import cases as C
 
     M = C.namespace("torchfsm")
-    enums = {
-        "setdrk1": SETDRKIntegrator.SETDRK1,
-        "setdrk2": SETDRKIntegrator.SETDRK2,
-        "setdrk3": SETDRKIntegrator.SETDRK3,
-        "setdrk4": SETDRKIntegrator.SETDRK4,
-        "etdrk0": ETDRKIntegrator.ETDRK0,
-        "etdrk1": ETDRKIntegrator.ETDRK1,
-        "etdrk2": ETDRKIntegrator.ETDRK2,
-    }
     only = set(sys.argv[2:])
     for name, case in C.CASES.items():
         if only and name not in only:

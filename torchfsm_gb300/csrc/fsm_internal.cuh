@@ -77,7 +77,7 @@ int split_parts(const FsmPlan* p, int batch);
 
 // Raise a kernel's dynamic shared-memory limit when it needs more than 48 KB. The
 // attribute is per function and per device; the size set is remembered per
-// (kernel, device) so that repeated launches skip the driver call.
+// (kernel, device) so that repeated launches skip the attribute call.
 bool smem_attr_known(const void* kernel, int device, size_t smem);
 void smem_attr_record(const void* kernel, int device, size_t smem);
 

@@ -9,8 +9,8 @@ integration_radius=.., cpu_cached=..)`` accepts the reference's options;
 the device in FP64). ``RKIntegrator`` members select the explicit Runge-Kutta
 schemes of integrator/_rk.py with a fixed step on the full right-hand side
 L u + N(u) (operator/_base.py:408-431, 492-502); ``adaptive=True`` (step-size
-control by an error estimate with a host decision per trial step,
-integrator/_rk.py:60-79) is not provided and raises NotImplementedError.
+control, integrator/_rk.py:60-79) raises NotImplementedError, as the reference's own
+adaptive step does on spectral states (it takes torch.max of a complex tensor).
 """
 
 from enum import Enum

@@ -757,7 +757,6 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   // plane (2D) / volume (3D) passes
   float2* arr = (float2*)(ws + off_arrays);
   a.slots = nullptr;
-  const bool ks_mean = p->nl == FSM_NL_KS && (p->flags & FSM_FLAG_REMOVE_MEAN);
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   if ((rc = cuda_check(cudaStreamIsCapturing(st, &cap), "stream capture query"))) return rc;
   // Large batches run in parts on streams forked from the caller's: the parts' launches

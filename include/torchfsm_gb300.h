@@ -180,8 +180,9 @@ int fsm_integrate_profiled(const FsmPlan* plan, int32_t batch, void* state, int3
  * by every GPU that loads it until the process exits; the caller still passes
  * the plan (created beforehand; plan creation allocates) and the state. Work
  * whose scratch would exceed the array (fsm_plan_workspace_bytes) is rejected
- * with FSM_ERR_INVALID. The first call on a device looks up the array's device
- * address and must come before any stream capture on that device. All calls
+ * with FSM_ERR_INVALID. It runs one launch sequence on `stream` (never the
+ * library's own streams of a split batch). The first call on a device looks up
+ * the array's device address and must come before any stream capture on that device. All calls
  * share the one array: calls that overlap on the GPU (other streams, other
  * threads) race and corrupt each other's results; serialise them. No
  * counterpart in the reference. */

@@ -684,7 +684,8 @@ struct PlaneSequence {
 };
 
 int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
-                   int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof) {
+                   int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof,
+                   bool allow_split = true) {
   if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
   size_t off_arrays = 0;
   const size_t need = workspace_layout(p, batch, steps, &off_arrays);
@@ -764,7 +765,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   // which fills the SMs better than one launch sequence of the whole batch.
   // Samples are independent except under the KS batch-wide mean; capture and the profiled
   // (per-launch timed) call keep one sequence.
-  const int NP = (prof || cap != cudaStreamCaptureStatusNone) ? 1 : fsm::split_parts(p, batch);
+  const int NP = (!allow_split || prof || cap != cudaStreamCaptureStatusNone) ? 1 : fsm::split_parts(p, batch);
   const bool split = NP > 1;
   if (!split) {
     PlaneSequence q{p, batch_arrays(p, a, arr, 0, batch), record_slot, steps, st, prof};
@@ -811,7 +812,8 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
 namespace fsm {
 int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
                              size_t workspace_bytes, cudaStream_t st) {
-  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr);
+  // one launch sequence on the caller's stream: no library streams for allocation-free callers
+  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr, false);
 }
 }  // namespace fsm
 

@@ -201,6 +201,23 @@ int fsm_irfftn(const FsmPlan* plan, int32_t count, void* in, float* out, void* s
  * a NaN or Inf and 0 otherwise (device int32 array). */
 int fsm_nonfinite_flags(const FsmPlan* plan, int32_t count, const void* fields, int32_t* flags, void* stream);
 
+/* Elementwise kernels of the hand-written SETDRK4 adjoint (gradients of integrate; no
+ * counterpart in the reference, which differentiates its loop with torch autograd,
+ * operator/_base.py:731-735). All arrays are device arrays, launched on `stream`.
+ * fsm_adj_accumulate: tbar[i] += Re(conj(x[i]) y[i]), i < n (x, y complex64, tbar float64).
+ * fsm_adj_vjp_products: the physical-space products of the Convection vector-Jacobian
+ *   product for `batch` samples of `points` grid points and nd = C channels: w_c = scale
+ *   nbar_c, ubar_c = sum_c' w_c' g_c[c'] (g_c = d_c u, arrays [batch][C][points]),
+ *   uw[i][b][c] = u_i w_c ([nd][batch][C][points]).
+ * fsm_adj_vjp_combine: out = m (sub - i sum_i k_i suw[i]) over [batch_channels][points]
+ *   half-spectrum points (sub, out complex64; suw [nd][batch_channels][points]; k_i and m
+ *   float [points]). */
+int fsm_adj_accumulate(int64_t n, const void* x, const void* y, double* tbar, void* stream);
+int fsm_adj_vjp_products(int32_t batch, int32_t nd, int64_t points, float scale, const float* nbar, const float* u,
+                         const float* g0, const float* g1, const float* g2, float* ubar, float* uw, void* stream);
+int fsm_adj_vjp_combine(int32_t batch_channels, int32_t nd, int64_t points, const void* sub, const void* suw,
+                        const float* k0, const float* k1, const float* k2, const float* m, void* out, void* stream);
+
 /* Copy the message of the last failure on this host thread into buf. */
 int fsm_last_error(char* buf, size_t len);
 

@@ -66,6 +66,9 @@ EXPORTS = (
     "fsm_rfftn",
     "fsm_irfftn",
     "fsm_nonfinite_flags",
+    "fsm_adj_accumulate",
+    "fsm_adj_vjp_products",
+    "fsm_adj_vjp_combine",
     "fsm_last_error",
     "fsm_abi_version",
 )
@@ -143,6 +146,9 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_rfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_irfftn.argtypes = [vp, i32, vp, vp, vp]
         lib.fsm_nonfinite_flags.argtypes = [vp, i32, vp, vp, vp]
+        lib.fsm_adj_accumulate.argtypes = [i64, vp, vp, vp, vp]
+        lib.fsm_adj_vjp_products.argtypes = [i32, i32, i64, ctypes.c_float, vp, vp, vp, vp, vp, vp, vp, vp]
+        lib.fsm_adj_vjp_combine.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp]
         lib.fsm_last_error.argtypes = [ctypes.c_char_p, sz]
         for name in EXPORTS:
             getattr(lib, name).restype = ctypes.c_int

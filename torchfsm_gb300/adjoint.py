@@ -115,6 +115,13 @@ class ConvectionAdjoint:
         tabs = _contour_tables(L.to(torch.complex128), dt, M, r)
         self.tabs = [t.to(torch.float32) for t in tabs]  # E, E2, c1, c4, c5, c6
         self.dtabs = _table_derivatives(L.to(torch.complex128), dt, M, r)
+        # dense per-point wavenumbers and mask / N_tot over the half spectrum, for the fused
+        # vector-Jacobian-product combination
+        half = [1, 1] + [n for n in shape[:-1]] + [h]
+        self.k_dense = [torch.broadcast_to(k, half).reshape(-1).contiguous() for k in ks]
+        self.m_dense = torch.broadcast_to(m / self.ntot, half).reshape(-1).contiguous().to(torch.float32)
+        self.points = int(math.prod(shape))
+        self.half_points = int(math.prod(shape[:-1])) * h
 
     # -- transforms --------------------------------------------------------
     def _phys(self, half):
@@ -142,13 +149,25 @@ class ConvectionAdjoint:
 
     def nonlinear_vjp(self, a, nbar, fields=None):
         u, g = fields if fields is not None else self._fields(a)
-        w = (self.coef * self.ntot) * self._phys(nbar)        # [B, C, ...]
-        # ubar_c = sum_c' w_c' d_c u_c'
-        ubar = torch.stack([(w * g[c]).sum(1) for c in range(self.nd)], dim=1)
-        out = self._spec(ubar)
-        for i in range(self.nd):
-            out = out - 1j * self.k[i] * self._spec(u[:, i:i + 1] * w)
-        return out * (self.mask / self.ntot)
+        lib = _lib.load()
+        stream = torch.cuda.current_stream(nbar.device).cuda_stream
+        nb = self._phys(nbar)                                  # [B, C, ...]; w = coef N_tot nb
+        B, C = nb.shape[0], nb.shape[1]
+        # ubar_c = sum_c' w_c' d_c u_c' and u_i w_c in one pass over the grid
+        ubar = torch.empty_like(nb)
+        uw = torch.empty((self.nd,) + tuple(nb.shape), dtype=nb.dtype, device=nb.device)
+        gp = [x.data_ptr() for x in g] + [None] * (3 - self.nd)
+        _lib.check(lib.fsm_adj_vjp_products(B, self.nd, self.points, self.coef * self.ntot, nb.data_ptr(),
+                                            u.data_ptr(), gp[0], gp[1], gp[2], ubar.data_ptr(), uw.data_ptr(),
+                                            stream))
+        s_ubar = self._spec(ubar)
+        s_uw = self._spec(uw.reshape((self.nd * B,) + tuple(nb.shape[1:])))
+        # (mask / N_tot) (rfft(ubar) - i sum_i k_i rfft(u_i w))
+        out = torch.empty_like(s_ubar)
+        kp = [x.data_ptr() for x in self.k_dense] + [None] * (3 - self.nd)
+        _lib.check(lib.fsm_adj_vjp_combine(B * C, self.nd, self.half_points, s_ubar.data_ptr(), s_uw.data_ptr(),
+                                           kp[0], kp[1], kp[2], self.m_dense.data_ptr(), out.data_ptr(), stream))
+        return out
 
     # -- one SETDRK4 step and its adjoint --------------------------------------
     def step_adjoint(self, u, ubar_next, tbar):
@@ -163,8 +182,10 @@ class ConvectionAdjoint:
         n3 = self.nonlinear(a3, fl)
 
         def acc(t, x, y):
-            if tbar is not None:
-                tbar[t] += (x.conj() * y).real.double()
+            if tbar is not None:  # tbar[t] += Re(conj(x) y), fused
+                x, y = x.contiguous(), y.contiguous()
+                _lib.check(_lib.load().fsm_adj_accumulate(x.numel(), x.data_ptr(), y.data_ptr(), tbar[t].data_ptr(),
+                                                          torch.cuda.current_stream(x.device).cuda_stream))
 
         ub = ubar_next
         u_bar = E * ub

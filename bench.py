@@ -741,6 +741,20 @@ def ncu_case(workload: str = "ns2d", n3d: int = 256):
     entry.build()
     from torchfsm_gb300 import initial, pde
 
+    if workload == "burgers2d_grad":
+        # the differentiable workload's shapes (128^2 x 16, 2 channels), 10 steps, forward + backward
+        from torchfsm_gb300.operator import Convection, Laplacian
+
+        device = torch.device("cuda", 0)
+        u0 = torch.tensor(initial.band_limited((128, 128), 16, 2, 6, SEED, 1.0).astype(np.float32), device=device)
+        nu = torch.tensor(0.01, device=device, requires_grad=True)
+        op = nu * Laplacian() - Convection()
+        u = u0.clone().requires_grad_(True)
+        out = op.integrate(u_0=u, mesh=[(0.0, 2 * math.pi, 128)] * 2, dt=0.005, step=10)
+        (out ** 2).mean().backward()
+        torch.cuda.synchronize()
+        print("ncu case done", bool(torch.isfinite(u.grad).all().item()))
+        return
     if workload == "burgers3d":
         n = n3d
         device = torch.device("cuda", 0)

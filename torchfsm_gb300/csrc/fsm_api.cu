@@ -243,6 +243,7 @@ static void free_plan(FsmPlan* p) {
   if (!p) return;
   cudaFree(p->kvec);
   cudaFree(p->keep);
+  cudaFree(p->tile_zero);
   cudaFree(p->tw);
   cudaFree(p->tab);
   cudaFree(p->source);
@@ -382,11 +383,26 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       if (prog->keep[i]) keep[p->koff[i] + j] = prog->keep[i][j] ? 1 : 0;
     }
   }
+  // Column tiles of the register axis-0 pass (2D column pass, 3D x pass) whose inner columns
+  // are all dealiased: the fields built from the masked state are zero there.
+  std::vector<uint8_t> tile_zero;
   {
-    // the trailing run of dealiased entries of the last axis' half spectrum
-    const int last = nd - 1, h = mesh->n[last] / 2 + 1;
-    p->ycut = h;
-    while (p->ycut > 0 && keep[p->koff[last] + p->ycut - 1] == 0) --p->ycut;
+    const int n0 = mesh->n[0];
+    const int w = n0 == 256 ? 16 : (n0 == 128 || n0 == 64) ? 32 : (n0 == 32 || n0 == 16) ? 64 : 0;
+    if (w && (path == 2 || path == 4)) {
+      const int h = mesh->n[nd - 1] / 2 + 1;
+      const int64_t inner = p->S / n0;
+      auto kept = [&](int64_t j) {
+        if (nd == 2) return keep[p->koff[1] + j] != 0;
+        return keep[p->koff[1] + j / h] != 0 && keep[p->koff[2] + j % h] != 0;
+      };
+      tile_zero.resize((size_t)((inner + w - 1) / w));
+      for (size_t t = 0; t < tile_zero.size(); ++t) {
+        bool any = false;
+        for (int64_t j = (int64_t)t * w; j < (int64_t)(t + 1) * w && j < inner; ++j) any = any || kept(j);
+        tile_zero[t] = any ? 0 : 1;
+      }
+    }
   }
   std::vector<float2> tw(kTwiddleMax);
   for (int k = 0; k < kTwiddleMax; ++k) {
@@ -399,6 +415,13 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       (rc = cuda_check(cudaMalloc(&p->keep, total_k), "cudaMalloc keep")) ||
       (rc = cuda_check(cudaMalloc(&p->tw, kTwiddleMax * sizeof(float2)), "cudaMalloc twiddles")) ||
       (rc = cuda_check(cudaMalloc(&p->tab, tab_bytes), "cudaMalloc tables"))) {
+    free_plan(p);
+    return rc;
+  }
+  if (!tile_zero.empty() &&
+      ((rc = cuda_check(cudaMalloc(&p->tile_zero, tile_zero.size()), "cudaMalloc tile flags")) ||
+       (rc = cuda_check(cudaMemcpyAsync(p->tile_zero, tile_zero.data(), tile_zero.size(), cudaMemcpyHostToDevice, st),
+                        "copy tile flags")))) {
     free_plan(p);
     return rc;
   }
@@ -732,8 +755,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.keepx = p->keep + p->koff[0];
   a.keepy = p->keep + p->koff[p->ndim - 1];
   a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
-  a.ycut = p->ycut;
-  a.prune = p->path == 2 ? 1 : 0;
+  a.tile_zero = p->tile_zero;
   a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
   a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));

@@ -320,7 +320,9 @@ struct FsmPlan {
   // fused-path array counts per sample (2D / 3D)
   int n_mid = 0, n_prod = 0, n_aux = 0, n_mid2 = 0;
   int path = 0;  // 1: line kernel (1D), 2: plane passes (2D), 3: pointwise, 4: volume passes (3D)
-  int ycut = 0;  // last-axis half-spectrum entries [ycut, n/2+1) are all dealiased to zero
+  // per column tile of the register axis-0 pass (W adjacent inner columns): 1 where every column
+  // is dealiased, so that the next-stage fields built there are zero (null: no such pass)
+  uint8_t* tile_zero = nullptr;
 };
 
 namespace fsm {

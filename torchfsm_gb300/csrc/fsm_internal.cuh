@@ -42,8 +42,7 @@ struct StepArgs {
   int flags;
   int64_t S;
   int H;
-  int ycut;   // last-axis entries at or above ycut are zero in every field built from the masked state
-  int prune;  // 2D register column pass: tiles at or above ycut write zero fields without transforms
+  const uint8_t* tile_zero;  // register axis-0 pass: column tiles whose next-stage fields are zero
 };
 
 int transform_r2c_last(int n, const float* in, float2* out, int64_t rows, const float2* tw, cudaStream_t st);

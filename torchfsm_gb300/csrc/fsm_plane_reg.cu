@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
       axis0_update<NX, KIND, DIM, -1, -1>(a, tileA, b, c0, cg, last);
     }
     if (!a.emit) continue;  // uniform: no further barriers in this group
-    if (DIM == 2 && a.prune && c0 >= a.ycut) {
+    if (a.tile_zero && a.tile_zero[blockIdx.x]) {
       // every column of this tile is dealiased: the next-stage fields are zero here, written
       // directly (coalesced rows of W columns) without the transforms
       constexpr int NMO = (KIND == FSM_NL_CONVECTION) ? 2 : K::NMG;  // fields of this channel group

@@ -836,7 +836,7 @@ def main():
                 "config": {"workload": WORKLOAD, "grid": [N, N], "batch": BATCH, "time_steps": TIME_STEPS,
                            "dt": DT, "nu": 1.0 / RE, "integrator": "SETDRK4", "sample": r["sample"],
                            "l2": "n/a (host)"},
-                "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": dict({k: r[k] for k in ("unit", "cores", "kind", "sample")}, value=value),
                 "e2e": {"value": value, "unit": "DOF*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return

@@ -218,6 +218,61 @@ int fsm_adj_vjp_products(int32_t batch, int32_t nd, int64_t points, float scale,
 int fsm_adj_vjp_combine(int32_t batch_channels, int32_t nd, int64_t points, const void* sub, const void* suw,
                         const float* k0, const float* k1, const float* k2, const float* m, void* out, void* stream);
 
+/* Serving engine: a slot pool of one plan advancing many independent solve requests together
+ * (continuous batching). No counterpart in the reference, whose Operator.integrate
+ * (operator/_base.py:676-751) solves one batch at a time with one dt; each request here is
+ * that solve with its own batch, step count and dt.
+ *
+ * fsm_serve_create: `plan` built with table_batch >= capacity (each slot has its own dt);
+ *   `state` DEVICE complex64 [capacity][C][S]; `workspace` DEVICE of at least
+ *   fsm_plan_workspace_bytes(plan, capacity, chunk) bytes; all work runs on `stream`. flags:
+ *   FSM_SERVE_GRAPHS replays ticks of at most 64 steps as CUDA graphs (captured per
+ *   (occupied slots, steps), step counts of such ticks rounded down to a power of two).
+ *   tick_ms > 0 bounds a tick to about that much device time (from the measured time per step
+ *   and slot); 0: ticks of up to `chunk` steps. The engine keeps the pointers; it allocates no
+ *   device memory. Plans whose samples interact (KS with the batch-wide mean) are refused.
+ * fsm_serve_submit: queue a request of `batch` samples: u0 DEVICE [batch][C][S] half spectra,
+ *   read when the request is admitted; out DEVICE [batch][C][S], written when it leaves (u0 and
+ *   out may be the same buffer). Both must stay valid until the request has left. Ids are the
+ *   caller's and unique among pending requests.
+ * fsm_serve_tick: if no tick is in flight, admit waiting requests in submission order while the
+ *   head of the queue fits into the free slots, then launch k steps of every occupied slot
+ *   (k = the fewest remaining steps, at most chunk and the tick_ms bound). *steps_launched = k,
+ *   0 when a tick is in flight or no slot is occupied.
+ * fsm_serve_poll: complete the tick in flight once the device has finished it (wait != 0:
+ *   block until then). Completed requests copy their slots to `out` (on the stream: the results
+ *   are ready for work enqueued on it after this call) and leave; the remaining slots are
+ *   compacted. Up to max_ids ids of completed requests are reported in done_ids (the rest at
+ *   the next poll); *in_flight = 1 while a tick is still running.
+ * fsm_serve_cancel: a waiting request is dropped (u0, out untouched); an active one leaves at
+ *   once, or when the tick in flight completes, writing the state it reached to `out`; it is
+ *   not reported by fsm_serve_poll.
+ * fsm_serve_request_status: FSM_SERVE_WAITING / ACTIVE / DONE (completed, not yet reported) or
+ *   FSM_SERVE_UNKNOWN, and the steps still to run.
+ * fsm_serve_stats: up to n of {occupied slots, waiting requests, active requests, tick in
+ *   flight, ticks, kernel launches, graph replays, slot-steps launched, completed, cancelled}.
+ * fsm_serve_destroy: waits for the stream, releases the graphs and events.
+ * One engine is used by one host thread at a time (calls are serialised by a lock); engines on
+ * different streams run concurrently. */
+typedef struct FsmServe FsmServe;
+#define FSM_SERVE_GRAPHS 1
+#define FSM_SERVE_UNKNOWN (-1)
+#define FSM_SERVE_WAITING 0
+#define FSM_SERVE_ACTIVE 1
+#define FSM_SERVE_DONE 2
+#define FSM_SERVE_NSTATS 10
+int fsm_serve_create(FsmPlan* plan, int32_t capacity, int32_t chunk, void* state, void* workspace,
+                     size_t workspace_bytes, int32_t flags, double tick_ms, void* stream, FsmServe** out);
+int fsm_serve_submit(FsmServe* server, int64_t request_id, int32_t batch, int32_t steps, double dt, const void* u0,
+                     void* out);
+int fsm_serve_tick(FsmServe* server, int32_t* steps_launched);
+int fsm_serve_poll(FsmServe* server, int32_t wait, int64_t* done_ids, int32_t max_ids, int32_t* n_done,
+                   int32_t* in_flight);
+int fsm_serve_cancel(FsmServe* server, int64_t request_id);
+int fsm_serve_request_status(FsmServe* server, int64_t request_id, int32_t* status, int32_t* remaining);
+int fsm_serve_stats(FsmServe* server, int64_t* stats, int32_t n);
+int fsm_serve_destroy(FsmServe* server);
+
 /* Copy the message of the last failure on this host thread into buf. */
 int fsm_last_error(char* buf, size_t len);
 

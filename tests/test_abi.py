@@ -65,3 +65,21 @@ def test_invalid_arguments_return_status_without_gpu(libpath):
     prog.nonlinear = _lib.FSM_NL_VORTICITY  # needs 2D
     assert lib.fsm_plan_create(ctypes.byref(mesh), ctypes.byref(prog), 0.1, None, ctypes.byref(out)) == \
         _lib.FSM_ERR_INVALID
+
+
+def test_serving_engine_rejects_null_arguments_without_gpu(libpath):
+    lib = _lib.load(libpath)
+    out = ctypes.c_void_p()
+    assert lib.fsm_serve_create(None, 4, 8, None, None, 0, 0, 0.0, None, ctypes.byref(out)) == _lib.FSM_ERR_INVALID
+    assert "serve_create" in _lib.last_error()
+    assert lib.fsm_serve_submit(None, 1, 1, 1, 0.1, None, None) == _lib.FSM_ERR_INVALID
+    k = ctypes.c_int32()
+    assert lib.fsm_serve_tick(None, ctypes.byref(k)) == _lib.FSM_ERR_INVALID
+    n, busy = ctypes.c_int32(), ctypes.c_int32()
+    assert lib.fsm_serve_poll(None, 0, None, 0, ctypes.byref(n), ctypes.byref(busy)) == _lib.FSM_ERR_INVALID
+    assert lib.fsm_serve_cancel(None, 1) == _lib.FSM_ERR_INVALID
+    st = ctypes.c_int32()
+    assert lib.fsm_serve_request_status(None, 1, ctypes.byref(st), None) == _lib.FSM_ERR_INVALID
+    stats = (ctypes.c_int64 * _lib.FSM_SERVE_NSTATS)()
+    assert lib.fsm_serve_stats(None, stats, _lib.FSM_SERVE_NSTATS) == _lib.FSM_ERR_INVALID
+    assert lib.fsm_serve_destroy(None) == _lib.FSM_OK

@@ -40,7 +40,9 @@ def test_admission_respects_capacity_and_compacts():
     server = serving.SolveServer(device, hbm_budget_bytes=1 << 20, chunk=9, max_slots=40)
     server.run(reqs, realtime=False)
     for b in server.buckets.values():
-        assert b.n_active == 0 and all(o is None for o in b.owner)
+        st = b.engine.stats()
+        assert st["occupied"] == 0 and st["waiting"] == 0 and st["active"] == 0 and not b.pending
+        assert st["completed"] == sum(1 for r in reqs if (r.kind, r.n) == (b.kind, b.n))
     assert all(r.result is not None and r.t_done >= r.t_admit for r in reqs)
 
 

@@ -51,6 +51,13 @@ FSM_RK_FEHLBERG45 = 29
 FSM_RK_CASHKARP45 = 30
 FSM_APPLY = 40
 
+FSM_SERVE_GRAPHS = 1
+FSM_SERVE_UNKNOWN = -1
+FSM_SERVE_WAITING = 0
+FSM_SERVE_ACTIVE = 1
+FSM_SERVE_DONE = 2
+FSM_SERVE_NSTATS = 10
+
 # Every symbol the header declares; tests check that the library exports them.
 EXPORTS = (
     "fsm_plan_create",
@@ -69,6 +76,14 @@ EXPORTS = (
     "fsm_adj_accumulate",
     "fsm_adj_vjp_products",
     "fsm_adj_vjp_combine",
+    "fsm_serve_create",
+    "fsm_serve_submit",
+    "fsm_serve_tick",
+    "fsm_serve_poll",
+    "fsm_serve_cancel",
+    "fsm_serve_request_status",
+    "fsm_serve_stats",
+    "fsm_serve_destroy",
     "fsm_last_error",
     "fsm_abi_version",
 )
@@ -149,6 +164,15 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_adj_accumulate.argtypes = [i64, vp, vp, vp, vp]
         lib.fsm_adj_vjp_products.argtypes = [i32, i32, i64, ctypes.c_float, vp, vp, vp, vp, vp, vp, vp, vp]
         lib.fsm_adj_vjp_combine.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+        pi32, pi64 = ctypes.POINTER(i32), ctypes.POINTER(i64)
+        lib.fsm_serve_create.argtypes = [vp, i32, i32, vp, vp, sz, i32, ctypes.c_double, vp, ctypes.POINTER(vp)]
+        lib.fsm_serve_submit.argtypes = [vp, i64, i32, i32, ctypes.c_double, vp, vp]
+        lib.fsm_serve_tick.argtypes = [vp, pi32]
+        lib.fsm_serve_poll.argtypes = [vp, i32, pi64, i32, pi32, pi32]
+        lib.fsm_serve_cancel.argtypes = [vp, i64]
+        lib.fsm_serve_request_status.argtypes = [vp, i64, pi32, pi32]
+        lib.fsm_serve_stats.argtypes = [vp, pi64, i32]
+        lib.fsm_serve_destroy.argtypes = [vp]
         lib.fsm_last_error.argtypes = [ctypes.c_char_p, sz]
         for name in EXPORTS:
             getattr(lib, name).restype = ctypes.c_int

@@ -302,6 +302,86 @@ class NativePlan:
             workspace.data_ptr(), need, _stream(self.device)))
 
 
+class ServePool:
+    """The library's serving engine (``fsm_serve_*``) over one plan built with
+    ``table_batch >= capacity``: requests of half-spectrum samples are queued, admitted into
+    slots at tick boundaries, advanced together and written back in place when their steps
+    are done. All work runs on ``stream``; the state and workspace tensors are kept alive here."""
+
+    STATS = ("occupied", "waiting", "active", "in_flight", "ticks", "launches", "graph_replays",
+             "slot_steps", "completed", "cancelled")
+
+    def __init__(self, plan: NativePlan, capacity: int, chunk: int, stream: torch.cuda.Stream,
+                 graphs: bool = True, tick_ms: float = 0.0):
+        self.plan = plan
+        self.capacity, self.chunk = int(capacity), int(chunk)
+        self.stream = stream
+        shape = plan.shape
+        half = tuple(shape[:-1]) + (shape[-1] // 2 + 1,)
+        self.sample_shape = (plan.n_channel,) + half
+        self.handle = None
+        with torch.cuda.stream(stream):
+            self.state = torch.empty((self.capacity,) + self.sample_shape, dtype=torch.complex64, device=plan.device)
+            self.ws = torch.empty(plan.workspace_bytes(self.capacity, self.chunk), dtype=torch.uint8,
+                                  device=plan.device)
+        handle = ctypes.c_void_p()
+        _lib.check(_lib.load().fsm_serve_create(
+            plan.handle, self.capacity, self.chunk, self.state.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
+            _lib.FSM_SERVE_GRAPHS if graphs else 0, float(tick_ms), stream.cuda_stream, ctypes.byref(handle)))
+        self.handle = handle
+        self._ids = (ctypes.c_int64 * 256)()
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().fsm_serve_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def submit(self, rid: int, steps: int, dt: float, half: torch.Tensor) -> None:
+        """Queue ``half`` ([batch, C, ...] complex64 half spectra on the pool's device, written
+        stream-ordered on the pool's stream) for ``steps`` steps of ``dt``; the result replaces it."""
+        _require_cuda(half, "serve input")
+        if tuple(half.shape[1:]) != self.sample_shape or half.dtype != torch.complex64 or not half.is_contiguous():
+            raise _lib.FsmError(_lib.FSM_ERR_INVALID, f"serve input {tuple(half.shape)} for samples {self.sample_shape}")
+        _lib.check(_lib.load().fsm_serve_submit(self.handle, int(rid), half.shape[0], int(steps), float(dt),
+                                                half.data_ptr(), half.data_ptr()))
+
+    def tick(self) -> int:
+        """Admit what fits and launch the next tick; the steps launched (0: busy or idle)."""
+        k = ctypes.c_int32()
+        _lib.check(_lib.load().fsm_serve_tick(self.handle, ctypes.byref(k)))
+        return int(k.value)
+
+    def poll(self, wait: bool = False) -> Tuple[List[int], bool]:
+        """Complete the tick in flight if it is done (or wait for it): (completed ids, tick in flight)."""
+        lib = _lib.load()
+        ids: List[int] = []
+        n, busy = ctypes.c_int32(), ctypes.c_int32()
+        while True:
+            _lib.check(lib.fsm_serve_poll(self.handle, 1 if wait else 0, self._ids, len(self._ids), ctypes.byref(n),
+                                          ctypes.byref(busy)))
+            ids.extend(self._ids[i] for i in range(n.value))
+            if n.value < len(self._ids):
+                return ids, bool(busy.value)
+            wait = False
+
+    def cancel(self, rid: int) -> None:
+        _lib.check(_lib.load().fsm_serve_cancel(self.handle, int(rid)))
+
+    def status(self, rid: int) -> Tuple[int, int]:
+        st, rem = ctypes.c_int32(), ctypes.c_int32()
+        _lib.check(_lib.load().fsm_serve_request_status(self.handle, int(rid), ctypes.byref(st), ctypes.byref(rem)))
+        return int(st.value), int(rem.value)
+
+    def stats(self) -> dict:
+        arr = (ctypes.c_int64 * len(self.STATS))()
+        _lib.check(_lib.load().fsm_serve_stats(self.handle, arr, len(self.STATS)))
+        return dict(zip(self.STATS, list(arr)))
+
+
 def warn_precision(dtype: torch.dtype) -> None:
     global _WARNED_FP64
     if dtype == torch.float64 and not _WARNED_FP64:

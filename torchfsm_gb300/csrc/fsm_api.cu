@@ -255,6 +255,21 @@ static void free_plan(FsmPlan* p) {
 
 using namespace fsm;
 
+namespace fsm {
+int set_batch_dt_range(FsmPlan* p, int32_t b0, int32_t n, double dt, cudaStream_t st) {
+  if (!p || b0 < 0 || n < 1 || (int64_t)b0 + n > p->lin_batch || p->lin_batch < 2 || !(dt > 0.0))
+    return set_error(FSM_ERR_INVALID, "set_batch_dt arguments");
+  const int64_t per = (int64_t)p->lin_ch * p->S;
+  const int64_t lcount = (int64_t)p->lin_src_batch * per;
+  const int64_t count = per * n;
+  const int threads = 128;
+  k_phi_tables<<<(unsigned)((count + threads - 1) / threads), threads, 0, st>>>(
+      p->lin, lcount, (int64_t)b0 * per, count, dt, p->integ, p->n_points, p->radius, phi_exact(p), p->tab,
+      p->tstride);
+  return cuda_check(cudaGetLastError(), "k_phi_tables (batch entries)");
+}
+}  // namespace fsm
+
 extern "C" {
 
 int fsm_abi_version(void) { return 1; }
@@ -468,13 +483,7 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
 }
 
 int fsm_plan_set_batch_dt(FsmPlan* p, int32_t b, double dt, void* stream) {
-  if (!p || b < 0 || b >= p->lin_batch || p->lin_batch < 2) return set_error(FSM_ERR_INVALID, "set_batch_dt arguments");
-  const int64_t per = (int64_t)p->lin_ch * p->S;
-  const int64_t lcount = (int64_t)p->lin_src_batch * per;
-  const int threads = 128;
-  k_phi_tables<<<(unsigned)((per + threads - 1) / threads), threads, 0, (cudaStream_t)stream>>>(
-      p->lin, lcount, (int64_t)b * per, per, dt, p->integ, p->n_points, p->radius, phi_exact(p), p->tab, p->tstride);
-  return cuda_check(cudaGetLastError(), "k_phi_tables (batch entry)");
+  return fsm::set_batch_dt_range(p, b, 1, dt, (cudaStream_t)stream);
 }
 
 int fsm_plan_move_batch(FsmPlan* p, int32_t dst, int32_t src, void* stream) {
@@ -832,6 +841,11 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
 }  // namespace
 
 namespace fsm {
+int integrate_on_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
+                           size_t workspace_bytes, cudaStream_t st) {
+  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr, true);
+}
+
 int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
                              size_t workspace_bytes, cudaStream_t st) {
   // one launch sequence on the caller's stream: no library streams for allocation-free callers

@@ -56,6 +56,12 @@ int launch_nonfinite(const float2* f, int64_t count, int64_t S, int32_t* flags, 
 int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
                              size_t workspace_bytes, cudaStream_t st);
 size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps);
+// fsm_integrate without recording on a caller-provided workspace; large batches may run in
+// parts on the library's streams (outside stream capture), as fsm_integrate does.
+int integrate_on_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
+                           size_t workspace_bytes, cudaStream_t st);
+// Recompute the coefficient tables of batch entries [b0, b0 + n) for time step dt (one launch).
+int set_batch_dt_range(FsmPlan* p, int32_t b0, int32_t n, double dt, cudaStream_t st);
 
 int transform_c2c_strided_reg(int n, bool inverse, float2* data, int64_t outer, int64_t inner, const float2* tw,
                               cudaStream_t st);  // -1: no register kernel for n

@@ -1,0 +1,337 @@
+// Serving engine: a slot pool of one plan advancing many independent solve requests together.
+//
+// The engine owns no device memory: the caller passes the slot-batched state [capacity][C][S]
+// and a workspace for (capacity, chunk). Requests are queued by fsm_serve_submit; each
+// fsm_serve_tick admits the waiting requests that fit (their initial spectra are copied into
+// their slots and their slots' coefficient tables recomputed for their dt), then launches k steps
+// of every occupied slot as one integration. Ticks of at most kGraphMaxSteps steps run as CUDA
+// graphs captured per (occupied slots, steps) on the shape's second occurrence, with the step
+// count rounded down to a power of two so that few shapes recur. fsm_serve_poll completes the
+// tick in flight: requests whose steps are done copy their slots to their output, leave, and the
+// remaining slots are compacted (fsm_serve_pool.h).
+//
+// Samples do not interact in these kernels, so a request's result does not depend on the other
+// requests in its ticks. The reference has no serving layer; each request is the solve of
+// Operator.integrate (operator/_base.py:676-751) with its own dt.
+#include <iterator>
+#include <list>
+#include <mutex>
+#include <unordered_map>
+#include <unordered_set>
+
+#include "fsm_internal.cuh"
+#include "fsm_serve_pool.h"
+
+namespace {
+
+constexpr int kGraphMaxSteps = 64;
+constexpr size_t kGraphCache = 48;
+
+}  // namespace
+
+struct FsmServe {
+  FsmPlan* plan = nullptr;
+  int32_t capacity = 0;
+  int32_t chunk = 0;
+  float2* state = nullptr;
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  int32_t flags = 0;
+  double tick_ms = 0.0;
+  cudaStream_t st = nullptr;
+  int device = 0;
+  int64_t sample = 0;  // complex values per sample (C * S)
+  fsm::SlotPool pool;
+  // tick in flight
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool in_flight = false;
+  int32_t tick_k = 0, tick_n = 0;
+  double step_ms = 0.0;  // device time per step and slot, running mean over ticks
+  // captured ticks, least recently used first
+  std::list<std::pair<uint64_t, cudaGraphExec_t>> lru;
+  std::unordered_map<uint64_t, std::list<std::pair<uint64_t, cudaGraphExec_t>>::iterator> graphs;
+  std::unordered_set<uint64_t> seen;
+  std::vector<int64_t> done_ids;  // completed, not yet reported
+  int64_t launches = 0, replays = 0, ticks = 0, slot_steps = 0, completed = 0, cancelled = 0;
+  std::mutex mu;
+
+  explicit FsmServe(int32_t cap) : pool(cap) {}
+};
+
+namespace {
+
+using fsm::cuda_check;
+using fsm::set_error;
+
+// Copy `count` samples starting at slot `slot` to (or from) a caller buffer.
+int copy_slots(FsmServe* s, int32_t slot, int32_t count, void* other, bool to_slots) {
+  const size_t bytes = (size_t)s->sample * count * sizeof(float2);
+  float2* slots = s->state + (int64_t)slot * s->sample;
+  return cuda_check(to_slots ? cudaMemcpyAsync(slots, other, bytes, cudaMemcpyDeviceToDevice, s->st)
+                             : cudaMemcpyAsync(other, slots, bytes, cudaMemcpyDeviceToDevice, s->st),
+                    "serve copy");
+}
+
+// Copy the samples of a request from its slots to its output, merging runs of adjacent slots.
+int copy_out(FsmServe* s, const fsm::ServeRequest* r) {
+  const int32_t n = (int32_t)r->slots.size();
+  int32_t i = 0;
+  while (i < n) {
+    int32_t j = i + 1;
+    while (j < n && r->slots[(size_t)j] == r->slots[(size_t)(j - 1)] + 1) ++j;
+    int rc = copy_slots(s, r->slots[(size_t)i], j - i, (float2*)r->out + (int64_t)i * s->sample, false);
+    if (rc) return rc;
+    i = j;
+  }
+  return FSM_OK;
+}
+
+// Requests leave: outputs written, slots freed and compacted (state and coefficient tables).
+int retire(FsmServe* s, const std::vector<fsm::ServeRequest*>& leaving) {
+  if (leaving.empty()) return FSM_OK;
+  int rc;
+  for (const fsm::ServeRequest* r : leaving)
+    if ((rc = copy_out(s, r))) return rc;
+  for (const fsm::SlotMove& m : s->pool.release(leaving)) {
+    if ((rc = copy_slots(s, m.dst, 1, s->state + (int64_t)m.src * s->sample, true))) return rc;
+    if ((rc = fsm_plan_move_batch(s->plan, m.dst, m.src, s->st))) return rc;
+  }
+  return FSM_OK;
+}
+
+void drop_graphs(FsmServe* s) {
+  for (auto& e : s->lru) cudaGraphExecDestroy(e.second);
+  s->lru.clear();
+  s->graphs.clear();
+}
+
+// k steps of slots [0, n): a graph replay when the shape has been captured, a capture on its
+// second occurrence (the first direct run has set the kernels' attributes), a direct run
+// otherwise. Returns the launches the device sees.
+int advance(FsmServe* s, int32_t n, int32_t k, int64_t* launches) {
+  const bool graphs = (s->flags & FSM_SERVE_GRAPHS) && k <= kGraphMaxSteps;
+  int rc;
+  if (graphs) {
+    const uint64_t key = ((uint64_t)(uint32_t)n << 32) | (uint32_t)k;
+    auto it = s->graphs.find(key);
+    if (it == s->graphs.end() && s->seen.count(key)) {
+      cudaGraph_t g = nullptr;
+      if ((rc = cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "serve capture")))
+        return rc;
+      const int irc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st);
+      const cudaError_t ec = cudaStreamEndCapture(s->st, &g);
+      if (irc) {
+        if (g) cudaGraphDestroy(g);
+        return irc;
+      }
+      if ((rc = cuda_check(ec, "serve end capture"))) return rc;
+      cudaGraphExec_t ex = nullptr;
+      rc = cuda_check(cudaGraphInstantiate(&ex, g, 0), "serve graph instantiate");
+      cudaGraphDestroy(g);
+      if (rc) return rc;
+      s->lru.emplace_back(key, ex);
+      it = s->graphs.emplace(key, std::prev(s->lru.end())).first;
+      while (s->lru.size() > kGraphCache) {
+        s->graphs.erase(s->lru.front().first);
+        cudaGraphExecDestroy(s->lru.front().second);  // freed once a replay in flight completes
+        s->lru.pop_front();
+      }
+    }
+    if (it != s->graphs.end()) {
+      s->lru.splice(s->lru.end(), s->lru, it->second);
+      if ((rc = cuda_check(cudaGraphLaunch(it->second->second, s->st), "serve graph launch"))) return rc;
+      ++s->replays;
+      return fsm_plan_launch_count(s->plan, 0, k, launches);
+    }
+    s->seen.insert(key);
+  }
+  if ((rc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st))) return rc;
+  return fsm_plan_launch_count(s->plan, n, k, launches);
+}
+
+// Complete the tick in flight if the device has finished it (or, with wait, once it has).
+int finish_tick(FsmServe* s, bool wait) {
+  if (!s->in_flight) return FSM_OK;
+  cudaError_t q = wait ? cudaEventSynchronize(s->e1) : cudaEventQuery(s->e1);
+  if (q == cudaErrorNotReady) return FSM_OK;
+  int rc;
+  if ((rc = cuda_check(q, "serve tick query"))) return rc;
+  float ms = 0.f;
+  if ((rc = cuda_check(cudaEventElapsedTime(&ms, s->e0, s->e1), "serve tick time"))) return rc;
+  const double per = (double)ms / ((double)s->tick_k * s->tick_n);
+  s->step_ms = s->step_ms > 0.0 ? 0.5 * (s->step_ms + per) : per;
+  s->in_flight = false;
+  std::vector<fsm::ServeRequest*> fin = s->pool.advance(s->tick_k);
+  std::vector<fsm::ServeRequest*> cancels = s->pool.pending_cancels();
+  std::vector<fsm::ServeRequest*> leaving = fin;
+  leaving.insert(leaving.end(), cancels.begin(), cancels.end());
+  if ((rc = retire(s, leaving))) return rc;
+  for (fsm::ServeRequest* r : fin) {
+    r->status = fsm::kServeDone;
+    s->done_ids.push_back(r->id);
+    ++s->completed;
+  }
+  for (fsm::ServeRequest* r : cancels) {
+    ++s->cancelled;
+    s->pool.erase(r->id);
+  }
+  return FSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fsm_serve_create(FsmPlan* plan, int32_t capacity, int32_t chunk, void* state, void* workspace,
+                     size_t workspace_bytes, int32_t flags, double tick_ms, void* stream, FsmServe** out) {
+  if (!plan || !out || capacity < 1 || chunk < 1 || !state || !workspace || tick_ms < 0.0)
+    return set_error(FSM_ERR_INVALID, "serve_create arguments");
+  if (plan->lin_batch < capacity || plan->lin_batch < 2)
+    return set_error(FSM_ERR_INVALID, "serve_create: the plan needs table_batch >= capacity (and >= 2)");
+  if (plan->source && plan->src_batch > 1)
+    return set_error(FSM_ERR_UNSUPPORTED, "serve_create: per-sample sources are not served");
+  if (plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN))
+    return set_error(FSM_ERR_UNSUPPORTED, "serve_create: the batch-wide mean couples the samples");
+  size_t need = 0;
+  int rc = fsm_plan_workspace_bytes(plan, capacity, chunk, &need);
+  if (rc) return rc;
+  if (workspace_bytes < need)
+    return set_error(FSM_ERR_INVALID, "serve_create: workspace too small: need " + std::to_string(need) + " bytes");
+  FsmServe* s = new FsmServe(capacity);
+  s->plan = plan;
+  s->capacity = capacity;
+  s->chunk = chunk;
+  s->state = (float2*)state;
+  s->ws = workspace;
+  s->ws_bytes = workspace_bytes;
+  s->flags = flags;
+  s->tick_ms = tick_ms;
+  s->st = (cudaStream_t)stream;
+  s->sample = (int64_t)plan->C * plan->S;
+  if ((rc = cuda_check(cudaGetDevice(&s->device), "serve device")) ||
+      (rc = cuda_check(cudaEventCreate(&s->e0), "serve event")) ||
+      (rc = cuda_check(cudaEventCreate(&s->e1), "serve event"))) {
+    if (s->e0) cudaEventDestroy(s->e0);
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return FSM_OK;
+}
+
+int fsm_serve_submit(FsmServe* s, int64_t request_id, int32_t batch, int32_t steps, double dt, const void* u0,
+                     void* out) {
+  if (!s || !u0 || !out) return set_error(FSM_ERR_INVALID, "serve_submit arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  if (s->pool.submit(request_id, batch, steps, dt, u0, out))
+    return set_error(FSM_ERR_INVALID, "serve_submit: duplicate id, batch outside [1, capacity], steps < 1 or dt <= 0");
+  return FSM_OK;
+}
+
+int fsm_serve_tick(FsmServe* s, int32_t* steps_launched) {
+  if (!s) return set_error(FSM_ERR_INVALID, "serve_tick arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  if (steps_launched) *steps_launched = 0;
+  if (s->in_flight) return FSM_OK;
+  int rc;
+  for (const fsm::ServeRequest* r : s->pool.admit()) {
+    const int32_t slot0 = r->slots.front();
+    if ((rc = copy_slots(s, slot0, r->batch, const_cast<void*>(r->u0), true))) return rc;
+    if ((rc = fsm::set_batch_dt_range(s->plan, slot0, r->batch, r->dt, s->st))) return rc;
+  }
+  const int32_t n = s->pool.occupied();
+  if (n == 0) return FSM_OK;
+  int32_t limit = 0;
+  if (s->step_ms > 0.0 && s->tick_ms > 0.0)
+    limit = (int32_t)std::max(1.0, std::min(1e9, s->tick_ms / (s->step_ms * n)));
+  int32_t k = s->pool.tick_steps(s->chunk, limit);
+  if ((s->flags & FSM_SERVE_GRAPHS) && k <= kGraphMaxSteps) {
+    int32_t p2 = 1;
+    while (p2 * 2 <= k) p2 *= 2;
+    k = p2;
+  }
+  if ((rc = cuda_check(cudaEventRecord(s->e0, s->st), "serve tick event"))) return rc;
+  int64_t launched = 0;
+  if ((rc = advance(s, n, k, &launched))) return rc;
+  if ((rc = cuda_check(cudaEventRecord(s->e1, s->st), "serve tick event"))) return rc;
+  s->in_flight = true;
+  s->tick_k = k;
+  s->tick_n = n;
+  s->launches += launched;
+  s->slot_steps += (int64_t)k * n;
+  ++s->ticks;
+  if (steps_launched) *steps_launched = k;
+  return FSM_OK;
+}
+
+int fsm_serve_poll(FsmServe* s, int32_t wait, int64_t* done_ids, int32_t max_ids, int32_t* n_done,
+                   int32_t* in_flight) {
+  if (!s || max_ids < 0 || (max_ids > 0 && !done_ids)) return set_error(FSM_ERR_INVALID, "serve_poll arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  int rc = finish_tick(s, wait != 0);
+  if (rc) return rc;
+  const int32_t n = (int32_t)std::min<size_t>((size_t)max_ids, s->done_ids.size());
+  for (int32_t i = 0; i < n; ++i) {
+    done_ids[i] = s->done_ids[(size_t)i];
+    s->pool.erase(done_ids[i]);
+  }
+  s->done_ids.erase(s->done_ids.begin(), s->done_ids.begin() + n);
+  if (n_done) *n_done = n;
+  if (in_flight) *in_flight = s->in_flight ? 1 : 0;
+  return FSM_OK;
+}
+
+int fsm_serve_cancel(FsmServe* s, int64_t request_id) {
+  if (!s) return set_error(FSM_ERR_INVALID, "serve_cancel arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  fsm::ServeRequest* r = s->pool.find(request_id);
+  if (!r || r->status == fsm::kServeDone) return set_error(FSM_ERR_INVALID, "serve_cancel: no such pending request");
+  if (s->pool.drop_waiting(request_id)) {
+    ++s->cancelled;
+    return FSM_OK;
+  }
+  if (s->in_flight) {  // leaves when the tick completes
+    r->cancel_pending = true;
+    return FSM_OK;
+  }
+  int rc = retire(s, {r});
+  if (rc) return rc;
+  ++s->cancelled;
+  s->pool.erase(request_id);
+  return FSM_OK;
+}
+
+int fsm_serve_request_status(FsmServe* s, int64_t request_id, int32_t* status, int32_t* remaining) {
+  if (!s || !status) return set_error(FSM_ERR_INVALID, "serve_request_status arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  const fsm::ServeRequest* r = s->pool.find(request_id);
+  *status = r ? r->status : fsm::kServeUnknown;
+  if (remaining) *remaining = r ? r->remaining : 0;
+  return FSM_OK;
+}
+
+int fsm_serve_stats(FsmServe* s, int64_t* stats, int32_t n) {
+  if (!s || !stats || n < 0) return set_error(FSM_ERR_INVALID, "serve_stats arguments");
+  std::lock_guard<std::mutex> g(s->mu);
+  const int64_t v[FSM_SERVE_NSTATS] = {s->pool.occupied(), s->pool.waiting(), s->pool.active_requests(),
+                                       s->in_flight ? 1 : 0, s->ticks, s->launches, s->replays, s->slot_steps,
+                                       s->completed, s->cancelled};
+  for (int32_t i = 0; i < n && i < FSM_SERVE_NSTATS; ++i) stats[i] = v[i];
+  return FSM_OK;
+}
+
+int fsm_serve_destroy(FsmServe* s) {
+  if (!s) return FSM_OK;
+  int rc;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    rc = cuda_check(cudaStreamSynchronize(s->st), "serve destroy");
+    drop_graphs(s);
+    cudaEventDestroy(s->e0);
+    cudaEventDestroy(s->e1);
+  }
+  delete s;
+  return rc;
+}
+
+}  // extern "C"

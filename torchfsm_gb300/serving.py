@@ -3,14 +3,16 @@
 Requests (PDE kind, grid size, batch, step count, dt, initial field) arrive
 over time. Requests of the same kind and grid size share a *bucket*: one
 plan whose coefficient tables have one entry per slot (each slot carries its
-own dt, set with ``fsm_plan_set_batch_dt``), one slot-batched spectral state
-and one workspace, sized at start-up from an HBM budget. Every *tick*
-advances all active slots of a bucket by up to ``chunk`` steps in one fused
-launch sequence (2D: one column + one row pass launch per stage for all
-slots; 1D: one launch); buckets tick on their own streams, so their work
-overlaps on the device. Between ticks finished requests leave (their slots
-are transformed back and copied to the host), the remaining slots are
-compacted, and waiting requests are admitted while slots are free.
+own dt) and the library's serving engine (``fsm_serve_*``, csrc/fsm_serve.cu)
+over one slot-batched spectral state and one workspace, sized at start-up
+from an HBM budget. The engine runs the scheduling in native code: every
+*tick* admits waiting requests while slots are free, then advances all
+occupied slots by up to ``chunk`` steps in one fused launch sequence (2D: one
+column + one row pass launch per stage for all slots; 1D: one launch), short
+ticks replayed as CUDA graphs; when a tick completes, finished requests write
+their slots back and leave, and the remaining slots are compacted. Buckets
+tick on their own streams, so their work overlaps on the device. Python turns
+requests into half spectra and results back into fields on the host.
 
 Per-sample arithmetic is independent of the other samples in the launch,
 so a request's result is the same alone and in the mix.
@@ -80,22 +82,23 @@ def slot_bytes(kind: str, n: int, chunk: int) -> int:
     return per_field * (C + 2 * C + 4 + C + 6)
 
 
-# Ticks of at most GRAPH_MAX_STEPS steps replay a CUDA graph captured per (active slots, steps);
-# the step count of such ticks is rounded down to a power of two so that few shapes recur.
+# Ticks of at most GRAPH_MAX_STEPS steps replay a CUDA graph captured per (occupied slots, steps);
+# the step count of such ticks is rounded down to a power of two so that few shapes recur
+# (the library's serving engine, fsm_serve_tick).
 GRAPH_MAX_STEPS = 64
-GRAPH_CACHE = 48
+# Requests handed to a bucket's engine ahead of admission (their half spectra wait on the device).
+ENGINE_QUEUE = 4
 
 
 class _Bucket:
+    """One (kind, n): a plan with one table entry per slot and the library's serving engine
+    (``fsm_serve_*``: admission, ticks, completion, slot compaction and graph replay run in
+    native code on the bucket's stream). Python transforms requests in and out of the half
+    spectrum and copies results to pinned host memory."""
+
     def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int,
                  priority: int = 0, tick_ms: float = 4.0, graphs: bool = True):
         self.kind, self.n, self.capacity, self.device, self.chunk = kind, n, capacity, device, chunk
-        self.tick_ms = tick_ms
-        self.use_graphs = graphs
-        self.graphs: "collections.OrderedDict[Tuple[int, int], torch.cuda.CUDAGraph]" = collections.OrderedDict()
-        self._seen: set = set()
-        self.replays = 0
-        self.step_ms: Optional[float] = None  # measured device time per step and slot
         op, mesh, C = problem(kind, n)
         self.C = C
         f_mesh = FourierMesh(mesh, device=device, dtype=torch.float32)
@@ -106,126 +109,66 @@ class _Bucket:
             self.plan = _native.NativePlan(prog, 0.05, _lib.FSM_SETDRK4, device,
                                            linear_coef64=op._linear_coef64(device), table_batch=capacity)
             self.sp = _native.Spectral(self.plan)
-            half = tuple(m[2] for m in mesh[:-1]) + (mesh[-1][2] // 2 + 1,)
-            self.state = torch.empty((capacity, C) + half, dtype=torch.complex64, device=device)
-            self.ws = torch.empty(self.plan.workspace_bytes(capacity, chunk), dtype=torch.uint8, device=device)
-        self.owner: List[Optional[Tuple[SolveRequest, int]]] = [None] * capacity
-        self.active: List[SolveRequest] = []
-        self.n_active = 0
-        self.tick: Optional[Tuple[torch.cuda.Event, torch.cuda.Event, int, int]] = None
-        self.launches = 0
+        self.engine = _native.ServePool(self.plan, capacity, chunk, self.stream, graphs=graphs, tick_ms=tick_ms)
+        self.pending: Dict[int, SolveRequest] = {}  # submitted to the engine, not yet completed
+        self.in_flight = False
 
-    def can_admit(self, req: SolveRequest) -> bool:
-        return self.tick is None and self.capacity - self.n_active >= req.batch
-
-    def admit(self, req: SolveRequest, now: float) -> None:
+    def submit(self, req: SolveRequest, now: float) -> None:
+        """Hand a request to the engine (it is admitted into slots at the engine's next tick)."""
         with torch.cuda.stream(self.stream):
             u = req.u0.to(self.device, non_blocking=True)
-            half = self.sp.to_half(u)
-            lo = self.n_active
-            self.state[lo:lo + req.batch].copy_(half)
-            for i in range(req.batch):
-                self.plan.set_batch_dt(lo + i, req.dt)
-                self.owner[lo + i] = (req, i)
-        req.slots = list(range(lo, lo + req.batch))
-        req.remaining = req.steps
+            req._half = self.sp.to_half(u).contiguous()
+        self.engine.submit(req.rid, req.steps, req.dt, req._half)
         req.t_admit = now
-        self.active.append(req)
-        self.n_active += req.batch
+        req.remaining = req.steps
+        self.pending[req.rid] = req
 
-    def launch(self) -> None:
-        k = min(self.chunk, min(r.remaining for r in self.active))
-        if self.step_ms:
-            # ticks of about tick_ms of device work keep admission and small requests responsive
-            k = max(1, min(k, int(self.tick_ms / (self.step_ms * self.n_active))))
-        if self.use_graphs and k <= GRAPH_MAX_STEPS:
-            k = 1 << (k.bit_length() - 1)
-        with torch.cuda.stream(self.stream):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e0.record(self.stream)
-            self._advance(self.n_active, k)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e1.record(self.stream)
-        # a captured tick (graph replay) runs one launch sequence; a direct one may run in parts
-        graphed = self.use_graphs and k <= GRAPH_MAX_STEPS and (self.n_active, k) in self.graphs
-        self.launches += self.plan.launch_count(k, 0 if graphed else self.n_active)
-        self.tick = (e0, e1, k, self.n_active)
+    def feed(self, queue: "collections.deque", now: float) -> None:
+        """Submit queued requests while the engine holds fewer than ENGINE_QUEUE waiting ones."""
+        waiting = self.engine.stats()["waiting"] if queue else 0
+        while queue and waiting < ENGINE_QUEUE:
+            self.submit(queue.popleft(), now)
+            waiting += 1
 
-    def _advance(self, n: int, k: int) -> None:
-        """k steps of slots [0, n) on the bucket's stream (the current stream here): a replay of the
-        graph of (n, k) when there is one. A shape is captured the second time it occurs (the first
-        run sets the kernels' attributes); the capture is thread-local, so the other buckets' host
-        threads keep launching meanwhile."""
-        if not self.use_graphs or k > GRAPH_MAX_STEPS:
-            self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
-            return
-        key = (n, k)
-        g = self.graphs.get(key)
-        if g is None:
-            if key not in self._seen:
-                self._seen.add(key)
-                self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
-                return
-            g = torch.cuda.CUDAGraph()
-            g.capture_begin(capture_error_mode="thread_local")
-            try:
-                self.plan.integrate_half(self.state[:n], k, workspace=self.ws)
-            finally:
-                g.capture_end()
-            self.graphs[key] = g
-            while len(self.graphs) > GRAPH_CACHE:
-                self.graphs.popitem(last=False)
-        else:
-            self.graphs.move_to_end(key)
-        g.replay()
-        self.replays += 1
+    def launch(self) -> int:
+        """The engine's next tick (admission + k steps of every occupied slot); k, 0 when idle or busy."""
+        k = self.engine.tick()
+        if k:
+            self.in_flight = True
+        return k
 
-    def poll(self) -> List[SolveRequest]:
-        """Finish the tick if the device is done with it; return the requests that completed, whose
+    def poll(self, wait: bool = False) -> List[SolveRequest]:
+        """Complete the tick if the device is done with it; return the requests that completed, whose
         results are being copied to pinned host memory (``r._copied`` records when)."""
-        if self.tick is None or not self.tick[1].query():
+        if not self.in_flight:
             return []
-        e0, e1, k, n = self.tick
-        self.tick = None
-        ms = e0.elapsed_time(e1) / (k * n)
-        self.step_ms = ms if self.step_ms is None else 0.5 * (self.step_ms + ms)
+        ids, self.in_flight = self.engine.poll(wait)
         done = []
-        for r in self.active:
-            r.remaining -= k
-            if r.remaining == 0:
-                done.append(r)
-        if not done:
-            return []
         with torch.cuda.stream(self.stream):
-            for r in done:
-                idx = torch.tensor(r.slots, device=self.device)
-                out = self.sp.to_physical(self.state.index_select(0, idx), keep_input=False)
+            for rid in ids:
+                r = self.pending.pop(rid)
+                out = self.sp.to_physical(r._half, keep_input=False)
+                r._half = None
+                r.remaining = 0
                 r.result = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
                 r.result.copy_(out, non_blocking=True)
                 r._copied = torch.cuda.Event()
                 r._copied.record(self.stream)
-        for r in done:
-            for s in r.slots:
-                self.owner[s] = None
-        self.active = [r for r in self.active if r.remaining > 0]
-        self._compact()
+                done.append(r)
         return done
 
-    def _compact(self) -> None:
-        """Move the highest occupied slots into freed holes so that slots [0, n_active) are occupied."""
-        occupied = [i for i in range(self.capacity) if self.owner[i] is not None]
-        n = len(occupied)
-        holes = [i for i in range(n) if self.owner[i] is None]
-        movers = [i for i in occupied if i >= n]
-        with torch.cuda.stream(self.stream):
-            for h, m in zip(holes, movers):
-                self.state[h].copy_(self.state[m])
-                self.plan.move_batch(h, m)
-                req, i = self.owner[m]
-                req.slots[i] = h
-                self.owner[h] = (req, i)
-                self.owner[m] = None
-        self.n_active = n
+    @property
+    def idle(self) -> bool:
+        st = self.engine.stats()
+        return not self.in_flight and st["occupied"] == 0 and st["waiting"] == 0
+
+    @property
+    def launches(self) -> int:
+        return self.engine.stats()["launches"]
+
+    @property
+    def replays(self) -> int:
+        return self.engine.stats()["graph_replays"]
 
 
 class SolveServer:
@@ -283,13 +226,10 @@ class SolveServer:
             copying = still
             for key, b in self.buckets.items():
                 copying.extend(b.poll())
-                if b.tick is None:
-                    q = waiting[key]
-                    while q and b.can_admit(q[0]):
-                        b.admit(q.popleft(), now())
-                    if b.n_active:
-                        b.launch()
-                if b.tick is not None:
+                b.feed(waiting[key], t)
+                if not b.in_flight:
+                    b.launch()
+                if b.in_flight:
                     busy = True
             if not busy:
                 time.sleep(0.0001)
@@ -320,21 +260,16 @@ class SolveServer:
                 with torch.cuda.device(device):
                     while True:
                         with cond:
-                            while not q and b.n_active == 0 and not state["arrived"]:
+                            while not q and b.idle and not state["arrived"]:
                                 cond.wait(0.01)
-                            batch = []
-                            while q and b.capacity - b.n_active - sum(r.batch for r in batch) >= q[0].batch:
-                                batch.append(q.popleft())
-                            finished = state["arrived"] and not q and b.n_active == 0 and not batch
+                            finished = state["arrived"] and not q and b.idle
                         if finished:
                             return
-                        for r in batch:
-                            b.admit(r, now())
-                        if b.n_active == 0:
-                            continue
+                        b.feed(q, now())  # only this worker takes from q
                         b.launch()
-                        b.tick[1].synchronize()
-                        for r in b.poll():
+                        if not b.in_flight:
+                            continue
+                        for r in b.poll(wait=True):
                             r._copied.synchronize()
                             r.t_done = now()
             except BaseException as e:  # surface worker failures to the caller

@@ -213,6 +213,21 @@ int fsm_nonfinite_flags(const FsmPlan* plan, int32_t count, const void* fields, 
  *   half-spectrum points (sub, out complex64; suw [nd][batch_channels][points]; k_i and m
  *   float [points]). */
 int fsm_adj_accumulate(int64_t n, const void* x, const void* y, double* tbar, void* stream);
+
+/* One step of the discrete adjoint of the plan's SETDRK4 step for a Convection program
+ * (integrator/_stable_etdrk/_setdrk_step.py:55-82 with operator/generic/_convection.py:43-46;
+ * the reference gets it from torch autograd, operator/_base.py:731-735). The plan must be
+ * SETDRK4, FSM_NL_CONVECTION with C == ndim, no source, and a real linear symbol (the tables
+ * are read as real). u: DEVICE [batch][C][S] state at the start of the step; ubar_next:
+ * cotangent of the state after it; ubar (output, may alias u or ubar_next): cotangent of u.
+ * Cotangents are half spectra v with dLoss = Re sum_k conj(v_k) du_k over the full spectrum.
+ * tbar (DEVICE float64 [6][batch][C][S], or NULL): tbar[t] += the cotangent of coefficient
+ * table t (E, E2, c1, c4, c5, c6) per mode. The forward stages are recomputed with the plan's
+ * own tables, so this is the exact adjoint of the forward the plan runs. Launches only (no
+ * allocation, no synchronisation): it may be captured into a CUDA graph. */
+int fsm_step_adjoint_workspace_bytes(const FsmPlan* plan, int32_t batch, size_t* bytes);
+int fsm_step_adjoint(const FsmPlan* plan, int32_t batch, const void* u, const void* ubar_next, void* ubar,
+                     double* tbar, void* workspace, size_t workspace_bytes, void* stream);
 int fsm_adj_vjp_products(int32_t batch, int32_t nd, int64_t points, float scale, const float* nbar, const float* u,
                          const float* g0, const float* g1, const float* g2, float* ubar, float* uw, void* stream);
 int fsm_adj_vjp_combine(int32_t batch_channels, int32_t nd, int64_t points, const void* sub, const void* suw,

@@ -83,3 +83,11 @@ def test_serving_engine_rejects_null_arguments_without_gpu(libpath):
     stats = (ctypes.c_int64 * _lib.FSM_SERVE_NSTATS)()
     assert lib.fsm_serve_stats(None, stats, _lib.FSM_SERVE_NSTATS) == _lib.FSM_ERR_INVALID
     assert lib.fsm_serve_destroy(None) == _lib.FSM_OK
+
+
+def test_step_adjoint_rejects_null_arguments_without_gpu(libpath):
+    lib = _lib.load(libpath)
+    n = ctypes.c_size_t()
+    assert lib.fsm_step_adjoint_workspace_bytes(None, 1, ctypes.byref(n)) == _lib.FSM_ERR_INVALID
+    assert lib.fsm_step_adjoint(None, 1, None, None, None, None, None, 0, None) == _lib.FSM_ERR_INVALID
+    assert "step_adjoint" in _lib.last_error()

@@ -52,3 +52,85 @@ def test_integrate_autograd_entry():
     loss.backward()
     err_nu = abs(nu.grad.item() - float(g["grad_nu"])) / abs(float(g["grad_nu"]))
     assert err_nu <= 1e-4
+
+
+def _torch_step_adjoint(adj, u, ub, tbar):
+    """One SETDRK4 adjoint step as tensor arithmetic (tables from the FP64 contour formulas, the
+    nonlinear term and its vector-Jacobian product from ConvectionAdjoint)."""
+    E, E2, c1, c4, c5, c6 = adj.tabs
+    fl = []
+    n0 = adj.nonlinear(u, fl)
+    a1 = E2 * u + c1 * n0
+    n1 = adj.nonlinear(a1, fl)
+    a2 = E2 * u + c1 * n1
+    n2 = adj.nonlinear(a2, fl)
+    a3 = E2 * a1 + c1 * (2 * n2 - n0)
+    n3 = adj.nonlinear(a3, fl)
+
+    def acc(t, x, y):
+        tbar[t] += (x.conj() * y).real.double()
+
+    u_bar = E * ub
+    acc(0, ub, u)
+    n0b = c4 * ub
+    acc(3, ub, n0)
+    n1b = 2 * c5 * ub
+    n2b = 2 * c5 * ub
+    acc(4, ub, 2 * (n1 + n2))
+    n3b = c6 * ub
+    acc(5, ub, n3)
+    a3b = adj.nonlinear_vjp(a3, n3b, fl[3])
+    a1b = E2 * a3b
+    acc(1, a3b, a1)
+    n2b = n2b + 2 * c1 * a3b
+    n0b = n0b - c1 * a3b
+    acc(2, a3b, 2 * n2 - n0)
+    a2b = adj.nonlinear_vjp(a2, n2b, fl[2])
+    u_bar = u_bar + E2 * a2b
+    acc(1, a2b, u)
+    n1b = n1b + c1 * a2b
+    acc(2, a2b, n1)
+    a1b = a1b + adj.nonlinear_vjp(a1, n1b, fl[1])
+    u_bar = u_bar + E2 * a1b
+    acc(1, a1b, u)
+    n0b = n0b + c1 * a1b
+    acc(2, a1b, n0)
+    return u_bar + adj.nonlinear_vjp(u, n0b, fl[0])
+
+
+@pytest.mark.parametrize("name", sorted(C.GRAD_CASES))
+def test_native_step_adjoint_matches_tensor_formulation(name):
+    """fsm_step_adjoint (fused kernels, the plan's tables) against the same step written as
+    FP32 tensor arithmetic: the state cotangent and the six table cotangents."""
+    from torchfsm_gb300 import adjoint
+
+    c = C.GRAD_CASES[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    dev = torch.device("cuda", 0)
+    op = c["nu"] * Laplacian() - Convection()
+    u0 = torch.tensor(g["u0"], dtype=torch.float32, device=dev)
+    with torch.no_grad():
+        op.integrate(u_0=u0, mesh=c["mesh"], dt=c["dt"], step=1)
+    plan = op._state_dict["integrator"].plan
+    h = plan.shape[-1] // 2 + 1
+    L64 = op._linear_coef64(dev)
+    L64 = L64.expand(L64.shape[:2] + tuple(plan.shape))[..., :h]
+    adj = adjoint.ConvectionAdjoint(plan, plan.program, L64, c["dt"])
+    u = adj.sp.to_half(u0).contiguous()
+    gen = torch.Generator().manual_seed(5)
+    ub = (adj.sp.to_half(torch.randn(tuple(u0.shape), generator=gen).to(dev)) / adj.ntot).contiguous()
+    tb_native = torch.zeros((6,) + tuple(u.shape), dtype=torch.float64, device=dev)
+    tb_torch = torch.zeros_like(tb_native)
+    out_native = adj.step_adjoint(u, ub, tb_native)
+    out_torch = _torch_step_adjoint(adj, u, ub, tb_torch)
+    torch.cuda.synchronize()
+
+    def rel(a, b):
+        return float((a - b).abs().pow(2).sum().sqrt() / b.abs().pow(2).sum().sqrt())
+
+    assert rel(out_native, out_torch) <= 1e-5
+    for t in range(6):
+        assert rel(tb_native[t], tb_torch[t]) <= 1e-5, t
+    # without table cotangents the state cotangent is the same
+    out2 = adj.step_adjoint(u, ub, None)
+    assert torch.equal(out2, out_native)

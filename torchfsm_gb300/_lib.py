@@ -76,6 +76,8 @@ EXPORTS = (
     "fsm_adj_accumulate",
     "fsm_adj_vjp_products",
     "fsm_adj_vjp_combine",
+    "fsm_step_adjoint_workspace_bytes",
+    "fsm_step_adjoint",
     "fsm_serve_create",
     "fsm_serve_submit",
     "fsm_serve_tick",
@@ -164,6 +166,8 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_adj_accumulate.argtypes = [i64, vp, vp, vp, vp]
         lib.fsm_adj_vjp_products.argtypes = [i32, i32, i64, ctypes.c_float, vp, vp, vp, vp, vp, vp, vp, vp]
         lib.fsm_adj_vjp_combine.argtypes = [i32, i32, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+        lib.fsm_step_adjoint_workspace_bytes.argtypes = [vp, i32, ctypes.POINTER(sz)]
+        lib.fsm_step_adjoint.argtypes = [vp, i32, vp, vp, vp, vp, vp, sz, vp]
         pi32, pi64 = ctypes.POINTER(i32), ctypes.POINTER(i64)
         lib.fsm_serve_create.argtypes = [vp, i32, i32, vp, vp, sz, i32, ctypes.c_double, vp, ctypes.POINTER(vp)]
         lib.fsm_serve_submit.argtypes = [vp, i64, i32, i32, ctypes.c_double, vp, vp]

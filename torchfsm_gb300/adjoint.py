@@ -26,13 +26,17 @@ accumulated per mode and contracted with dTable/dL * dL/dcoef, where the
 table derivatives come from the FP64 contour formulas (central differences
 in FP64).
 
-Spectral arithmetic of the backward pass runs as torch tensor operations on
-the GPU; every transform is the library's fsm_rfftn / fsm_irfftn. One adjoint
-step is captured as a CUDA graph and replayed for every step.
+One adjoint step is one call of the library's fsm_step_adjoint (the four
+stages recomputed with the plan's own tables and the library's transforms,
+the four vector-Jacobian products above, the backward recurrence and the
+table cotangents, about 50 launches); it is captured as a CUDA graph and
+replayed for every step. ``nonlinear`` / ``nonlinear_vjp`` state the same
+operations with tensor arithmetic for checking.
 """
 
 from __future__ import annotations
 
+import ctypes
 import math
 from typing import List, Optional, Sequence, Tuple
 
@@ -122,6 +126,7 @@ class ConvectionAdjoint:
         self.m_dense = torch.broadcast_to(m / self.ntot, half).reshape(-1).contiguous().to(torch.float32)
         self.points = int(math.prod(shape))
         self.half_points = int(math.prod(shape[:-1])) * h
+        self._ws = {}
 
     # -- transforms --------------------------------------------------------
     def _phys(self, half):
@@ -170,51 +175,28 @@ class ConvectionAdjoint:
         return out
 
     # -- one SETDRK4 step and its adjoint --------------------------------------
+    def _workspace(self, batch: int) -> torch.Tensor:
+        ws = self._ws.get(batch)
+        if ws is None:
+            n = ctypes.c_size_t()
+            _lib.check(_lib.load().fsm_step_adjoint_workspace_bytes(self.plan.handle, batch, ctypes.byref(n)))
+            ws = torch.empty(int(n.value), dtype=torch.uint8, device=self.plan.device)
+            self._ws[batch] = ws
+        return ws
+
     def step_adjoint(self, u, ubar_next, tbar):
-        E, E2, c1, c4, c5, c6 = self.tabs
-        fl = []  # physical fields of each stage input, reused by the vector-Jacobian products
-        n0 = self.nonlinear(u, fl)
-        a1 = E2 * u + c1 * n0
-        n1 = self.nonlinear(a1, fl)
-        a2 = E2 * u + c1 * n1
-        n2 = self.nonlinear(a2, fl)
-        a3 = E2 * a1 + c1 * (2 * n2 - n0)
-        n3 = self.nonlinear(a3, fl)
-
-        def acc(t, x, y):
-            if tbar is not None:  # tbar[t] += Re(conj(x) y), fused
-                x, y = x.contiguous(), y.contiguous()
-                _lib.check(_lib.load().fsm_adj_accumulate(x.numel(), x.data_ptr(), y.data_ptr(), tbar[t].data_ptr(),
-                                                          torch.cuda.current_stream(x.device).cuda_stream))
-
-        ub = ubar_next
-        u_bar = E * ub
-        acc(0, ub, u)
-        n0b = c4 * ub
-        acc(3, ub, n0)
-        n1b = 2 * c5 * ub
-        n2b = 2 * c5 * ub
-        acc(4, ub, 2 * (n1 + n2))
-        n3b = c6 * ub
-        acc(5, ub, n3)
-        a3b = self.nonlinear_vjp(a3, n3b, fl[3])
-        a1b = E2 * a3b
-        acc(1, a3b, a1)
-        n2b = n2b + 2 * c1 * a3b
-        n0b = n0b - c1 * a3b
-        acc(2, a3b, 2 * n2 - n0)
-        a2b = self.nonlinear_vjp(a2, n2b, fl[2])
-        u_bar = u_bar + E2 * a2b
-        acc(1, a2b, u)
-        n1b = n1b + c1 * a2b
-        acc(2, a2b, n1)
-        a1b = a1b + self.nonlinear_vjp(a1, n1b, fl[1])
-        u_bar = u_bar + E2 * a1b
-        acc(1, a1b, u)
-        n0b = n0b + c1 * a1b
-        acc(2, a1b, n0)
-        u_bar = u_bar + self.nonlinear_vjp(u, n0b, fl[0])
-        return u_bar
+        """Cotangent of the state at the start of a step from the cotangent after it; adds the
+        coefficient-table cotangents to ``tbar`` ([6, B, C, ...] float64) when given. One call of the
+        library's fsm_step_adjoint (the stages recomputed with the plan's own tables)."""
+        u = u.contiguous()
+        ubar_next = ubar_next.contiguous()
+        out = torch.empty_like(ubar_next)
+        ws = self._workspace(u.shape[0])
+        _lib.check(_lib.load().fsm_step_adjoint(
+            self.plan.handle, u.shape[0], u.data_ptr(), ubar_next.data_ptr(), out.data_ptr(),
+            tbar.data_ptr() if tbar is not None else None, ws.data_ptr(), ws.numel(),
+            torch.cuda.current_stream(u.device).cuda_stream))
+        return out
 
     def coef_gradient(self, tbar, symbol_half: torch.Tensor) -> torch.Tensor:
         """Sum over channels and modes (full spectrum) of tbar * dTable/dL * dL/dcoef, per batch entry."""
@@ -236,7 +218,7 @@ class _StepGraph:
         dev = like.device
         self.u_in = torch.zeros_like(like)
         self.v_in = torch.zeros_like(like)
-        scratch = [torch.zeros_like(t) for t in tbar] if tbar is not None else None
+        scratch = torch.zeros_like(tbar) if tbar is not None else None
         side = torch.cuda.Stream(dev)
         side.wait_stream(torch.cuda.current_stream(dev))
         with torch.cuda.stream(side):
@@ -282,7 +264,7 @@ class _IntegrateFn(torch.autograd.Function):
         want_coef = any(ctx.needs_input_grad[5:])
         tbar = None
         if want_coef:
-            tbar = [torch.zeros(v.shape, dtype=torch.float64, device=v.device) for _ in range(6)]
+            tbar = torch.zeros((6,) + tuple(v.shape), dtype=torch.float64, device=v.device)
         step = _StepGraph(adj, v, tbar) if steps > 1 else None
         starts = list(range(0, steps, K))
         for si in reversed(range(len(starts))):

@@ -116,8 +116,8 @@ class ConvectionAdjoint:
             w[-1] = 1.0
         self.weight = w
         L = L64_half.real.to(dev, torch.float64)
-        tabs = _contour_tables(L.to(torch.complex128), dt, M, r)
-        self.tabs = [t.to(torch.float32) for t in tabs]  # E, E2, c1, c4, c5, c6
+        self._L, self._M, self._r = L, M, r
+        self._tabs = None
         self.dtabs = _table_derivatives(L.to(torch.complex128), dt, M, r)
         # dense per-point wavenumbers and mask / N_tot over the half spectrum, for the fused
         # vector-Jacobian-product combination
@@ -127,6 +127,15 @@ class ConvectionAdjoint:
         self.points = int(math.prod(shape))
         self.half_points = int(math.prod(shape[:-1])) * h
         self._ws = {}
+
+    @property
+    def tabs(self):
+        """E, E2, c1, c4, c5, c6 from the FP64 contour formulas, rounded to FP32 (for the tensor
+        formulation; the library's step reads the plan's own tables)."""
+        if self._tabs is None:
+            tabs = _contour_tables(self._L.to(torch.complex128), self.dt, self._M, self._r)
+            self._tabs = [t.to(torch.float32) for t in tabs]
+        return self._tabs
 
     # -- transforms --------------------------------------------------------
     def _phys(self, half):

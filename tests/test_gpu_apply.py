@@ -72,3 +72,20 @@ def test_float64_input_returns_float64():
     u = torch.tensor(C.apply_input(name), dtype=torch.float64, device="cuda")
     out = pde.NavierStokesVorticity(100)(u=u, mesh=case["mesh"])
     assert out.dtype == torch.float64
+
+
+def test_run_operators_matches_individual_calls():
+    """run_operators shares one forward transform across the operators (operator/__init__.py of
+    the reference); each result equals the operator applied on its own."""
+    import torchfsm_gb300 as fsm
+
+    name = "apply_burgers2d_n32"
+    case = C.APPLY_CASES[name]
+    u = torch.tensor(C.apply_input(name), dtype=torch.float32, device="cuda")
+    ops = [pde.Burgers(0.01), fsm.Div(), fsm.Laplacian()]
+    outs = list(fsm.run_operators(u, ops, case["mesh"]))
+    singles = [pde.Burgers(0.01)(u=u, mesh=case["mesh"]), fsm.Div()(u=u, mesh=case["mesh"]),
+               fsm.Laplacian()(u=u, mesh=case["mesh"])]
+    for got, want in zip(outs, singles):
+        assert got.shape == want.shape
+        assert float((got - want).norm() / want.norm()) <= 1e-5

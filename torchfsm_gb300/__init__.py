@@ -8,6 +8,11 @@ CUDA kernels behind a C ABI (include/torchfsm_gb300.h).
 
 from . import functional, integrator, mesh, operator, pde, traj_recorder, utils
 from .mesh import FourierMesh, MeshGrid
-from .operator import Operator
+# the reference's package root re-exports its operator package (torchfsm/__init__.py)
+from .operator import (Biharmonic, ConservativeConvection, Convection, CoreGenerator, Curl, Div, ExplicitSource,
+                       Grad, ImplicitSource, KSConvection, Laplacian, LinearCoef, LinearOperator, NonlinearFunc,
+                       NonlinearOperator, NSPressureConvection, Operator, OperatorLike, SpatialDerivative,
+                       SpatialTensor, Velocity2Pressure, Vorticity2Pressure, Vorticity2Velocity, VorticityConvection,
+                       check_value_with_mesh, default, run_operators)
 
 __version__ = "0.1.0"

@@ -34,7 +34,7 @@ def _require_cuda(t: torch.Tensor, what: str) -> None:
     if not t.is_cuda:
         raise RuntimeError(
             f"torchfsm_gb300 runs on CUDA devices only: {what} is on {t.device}. "
-            "Move the initial condition to a CUDA device."
+            "Move it to a CUDA device (there is no CPU path)."
         )
 
 

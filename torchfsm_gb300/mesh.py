@@ -15,6 +15,7 @@ from typing import Optional, Sequence, Tuple, Union
 import numpy as np
 import torch
 
+from ._type import FourierTensor, SpatialTensor, ValueList  # noqa: F401
 from .utils import default, format_device_dtype
 
 MeshInfo = Sequence[Tuple[float, float, int]]

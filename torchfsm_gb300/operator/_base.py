@@ -456,9 +456,9 @@ class OperatorLike(_MutableMixIn):
 
         Programs the library lowers (the ones ``integrate`` runs fused) evaluate through the
         fused kernels: a one-step launch sequence of the FSM_APPLY scheme writes the
-        right-hand side over a half-spectrum copy of the (real) input. Other programs
-        (channel-changing post-processing cores, Python callables) evaluate their cores with
-        torch on the input's device."""
+        right-hand side over a half-spectrum copy of the (real) input; they need CUDA inputs.
+        Other programs (channel-changing post-processing cores, Python callables) evaluate their
+        cores with torch on the input's device."""
         if self._state_dict["f_mesh"] is None or mesh is not None:
             mesh, n_channel = self._pre_check(u, u_fft, mesh)
             self.register_mesh(mesh, n_channel)
@@ -484,10 +484,19 @@ class OperatorLike(_MutableMixIn):
         """(half spectrum of L u + N(u), its Spectral, the input's real dtype) through the library,
         or None where the program does not lower or the input is not on a CUDA device."""
         src = u if u is not None else u_fft
-        if src is None or not src.is_cuda or self._state_dict["apply_plan"] is False:
+        if src is None or self._state_dict["apply_plan"] is False:
             return None
         if any(isinstance(c, Tensor) and c.requires_grad for c, _ in self._linear_terms):
             return None  # keep autograd through torch for tensor coefficients that want gradients
+        if not src.is_cuda:
+            # programs the library covers run only there: no CPU evaluation of them
+            try:
+                _native.lower(self._linear_terms, self._nonlinear_funcs, self._state_dict["f_mesh"],
+                              self._state_dict["n_channel"], self._de_aliasing_rate)
+            except _lib.UnsupportedProgram:
+                self._state_dict["apply_plan"] = False
+                return None
+            _native._require_cuda(src, "the operator's input")
         plan = self._state_dict["apply_plan"]
         if plan is None or plan.device != src.device:
             f_mesh = self._state_dict["f_mesh"]

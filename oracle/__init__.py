@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY. Nothing in the product imports this package: only
 ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline``
-leg and its ``--impl reference`` arm) may import it, and only as the checker
-or as the timed CPU restatement of the reference.
+leg and its ``--impl reference`` arm) may import it, and only to compare
+results against it or as the timed CPU restatement of the reference.
 
 ``oracle.spectral`` restates, in numpy FP64 (complex128, full C2C spectra),
 the reference's mesh symbols, nonlinear cores, exponential-integrator

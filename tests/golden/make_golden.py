@@ -10,7 +10,7 @@ physical state and (where recorded) the physical trajectory are stored in
 ``<case>.npz``. ``phi_coefs.npz`` holds the reference's SETDRK4 / ETDRK
 coefficient tables for a few linear symbols and ``masks.npz`` its 2/3 dealias
 masks. These files are the pins of the numpy oracle and of the GPU path; the
-GPU machine never reads the reference itself.
+GPU tests never read the reference itself.
 """
 
 from __future__ import annotations

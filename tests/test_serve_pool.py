@@ -13,7 +13,7 @@ CSRC = os.path.join(os.path.dirname(HERE), "torchfsm_gb300", "csrc")
 
 
 @pytest.fixture(scope="module")
-def checker(tmp_path_factory):
+def pool_check_exe(tmp_path_factory):
     cxx = shutil.which("g++") or shutil.which("c++")
     if cxx is None:
         pytest.skip("no host C++ compiler")
@@ -24,6 +24,6 @@ def checker(tmp_path_factory):
 
 
 @pytest.mark.parametrize("seed", [1, 2, 3, 4])
-def test_slot_pool_invariants(checker, seed):
-    res = subprocess.run([checker, str(seed)], capture_output=True, text=True, timeout=120)
+def test_slot_pool_invariants(pool_check_exe, seed):
+    res = subprocess.run([pool_check_exe, str(seed)], capture_output=True, text=True, timeout=120)
     assert res.returncode == 0 and res.stdout.strip() == "ok", res.stdout + res.stderr

@@ -1,4 +1,4 @@
-"""Lowering of operators to the CUDA library and the fused integrate driver.
+"""Lowering of operators to the CUDA library and the fused integrate entry.
 
 An operator's (coefficient, core) list is lowered to a spectral program:
 the linear symbol L = sum coef * symbol evaluated in FP64 (any ``LinearCoef``

@@ -1,5 +1,5 @@
 // C ABI of torchfsm_gb300: plans, the FP64 coefficient kernel, the
-// integrate driver and the transforms. Declarations and the reference
+// integrate loop and the transforms. Declarations and the reference
 // interfaces each entry point replaces are in include/torchfsm_gb300.h.
 #include <math.h>
 #include <string.h>

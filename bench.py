@@ -380,6 +380,23 @@ def _pctl(xs, q):
     return xs[min(len(xs) - 1, int(round(q / 100.0 * (len(xs) - 1))))]
 
 
+# Nominal FP32 FMA rate of a GB300: 152 SMs x 128 FP32 lanes x 2 flop x 2.07 GHz.
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def fft_flop_fraction(n: int, channels: int, steps: int, device_ms: float) -> dict:
+    """FFT flops of a 1D SETDRK4 solve (per stage one inverse and one forward length-n complex
+    transform of the packed real fields, 5 n log2 n flops each, counted as the conventional
+    2.5 n log2 n per real transform: 12 real transforms per step, 30 log2 n flops per DOF*step)
+    against the nominal FP32 FMA rate."""
+    per_dof_step = 30.0 * math.log2(n)
+    flops = per_dof_step * n * channels * steps
+    achieved = flops / (device_ms * 1e-3) / 1e12
+    return {"fft_flops_per_dof_step": per_dof_step, "achieved_tflops": achieved,
+            "peak_tflops": FP32_NOMINAL_TFLOPS, "frac": achieved / FP32_NOMINAL_TFLOPS,
+            "peak_source": "nominal FP32 FMA rate (152 SMs x 128 lanes x 2 flop x 2.07 GHz)"}
+
+
 def run_burgers1d(args):
     """1D viscous Burgers, N = 128, nu = 0.01, L = 1, u0 = sin(2 pi x) + 0.5, dt = 0.01, 200 steps,
     batch 1, AutoRecorder (201 frames): solve latency through the public API."""
@@ -467,7 +484,8 @@ def run_burgers1d(args):
                     "d2h_bytes_per_step": out.numel() * 4},
             "gpu_launches": 1,
             "roofline": {"bound": "latency", "note": "one 128-point line per CTA; all 200 steps in one launch",
-                         "device_ms": statistics.median(dev)},
+                         "device_ms": statistics.median(dev),
+                         "fft_flop_fraction": fft_flop_fraction(n, 1, steps, statistics.median(dev))},
             "cpu_baseline": {"value": n * steps / cpu_s, "unit": "DOF*steps/s", "cores": 1, "kind": "port",
                              "sample": "the whole workload, numpy complex64 restatement, 1 thread"},
             "torch_gpu_reference": torch_ref}

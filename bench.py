@@ -48,6 +48,7 @@ SEED = 2024
 MESH = [(0.0, 2 * math.pi, N), (0.0, 2 * math.pi, N)]
 METRIC = "DOF*steps/s (2D NS vorticity 256^2 x 64, SETDRK4, FP32)"
 WORKLOAD = "ns2d_vorticity_256x256_b64_1000steps"
+FP64_SAMPLES = 4  # samples of the batch integrated again by the reference in float64 (accuracy leg)
 
 
 def _peaks():
@@ -236,9 +237,15 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
             return op.integrate(u_0=u_dev, dt=DT, step=k)
 
         torch_ref = torch_gpu_reference(device, w0, ours_half=ours_after)
+    # accuracy: the first samples of the e2e result against the reference's FP64 run of all 1000 steps
+    fp64 = None
+    if rank == 0 and not args.no_fp64_reference:
+        w = w0 if w0.ndim == 4 else w0[:, None]
+        fp64 = fp64_reference_rel_l2(lambda R: R.pde.NavierStokesVorticity(RE), MESH, w[:FP64_SAMPLES], DT,
+                                     TIME_STEPS, out_h[:FP64_SAMPLES], device)
     return {"ms": ms, "e2e_ms": e2e_ms, "finite": finite, "clocks": clk.summary(), "launches": launches_per_step,
             "prof": prof, "h2d": host_in.numel() * 4, "d2h": out_h.numel() * out_h.element_size(),
-            "B": B, "torch_ref": torch_ref}
+            "B": B, "torch_ref": torch_ref, "fp64": fp64}
 
 
 def _import_reference():
@@ -326,6 +333,37 @@ def torch_gpu_reference(device, w0: np.ndarray, ours_half=None, k1: int = 10, k2
         res["rel_l2_vs_fused_after_%d_steps" % k1] = float(
             torch.linalg.vector_norm(ours - out1) / torch.linalg.vector_norm(out1))
     return res
+
+
+def fp64_reference_rel_l2(make_op, mesh, u0: np.ndarray, dt: float, steps: int, ours, device) -> dict:
+    """Relative L2 distance of a result of ours from the reference's own integrator run in float64.
+
+    The unmodified reference (baseline/_ref) integrates ``u0`` with ``make_op(R).integrate`` in
+    float64 on ``device``: its mesh and coefficient tables follow the input's dtype
+    (``operator/_base.py:553-559``), so the transforms run in complex128 and the SETDRK4 contour
+    coefficients in FP64. ``ours`` is our FP32 result for the same initial field, mesh, dt and
+    step count. Any failure is reported as ``unavailable`` and leaves the rest of the line intact."""
+    import torch
+
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    try:
+        u = torch.tensor(np.asarray(u0, dtype=np.float64), device=device)
+        t0 = time.perf_counter()
+        ref = make_op(R).integrate(u_0=u, mesh=mesh, dt=dt, step=steps)
+        if ref.device.type == "cuda":
+            torch.cuda.synchronize(ref.device)
+        wall = time.perf_counter() - t0
+        if ref.dtype != torch.float64:
+            return {"unavailable": f"reference returned {ref.dtype}, not float64"}
+        ours64 = torch.as_tensor(ours).to(device=ref.device, dtype=torch.float64).reshape(ref.shape)
+        err = float(torch.linalg.vector_norm(ours64 - ref) / torch.linalg.vector_norm(ref))
+        return {"rel_l2": err, "samples": int(u.shape[0]), "steps": steps, "reference_wall_s": wall,
+                "kind": f"reference integrate in float64 (complex128 transforms) on {ref.device.type}",
+                "version": getattr(R, "__version__", "0.0.4")}
+    except Exception as e:  # noqa: BLE001 -- the accuracy leg must not cost the throughput line
+        return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
 def profile_kernels(plan, state0, ws, device) -> dict:
@@ -543,12 +581,20 @@ def run_burgers3d(args):
         torch_ref["unit"] = "DOF*steps/s"
         torch_ref["fused_device_over_reference"] = (dof_steps / (ms * 1e-3)) / torch_ref["value"]
         torch_ref["peak_mem_gb"] = torch.cuda.max_memory_allocated(device) / 1e9
+    # accuracy: our field after 50 steps against the reference's float64 run of the same 50 steps
+    fp64 = None
+    if not args.no_fp64_reference:
+        ours50 = op.integrate(u_0=u0, dt=dt, step=50)
+        fp64 = fp64_reference_rel_l2(lambda R: R.pde.Burgers(0.005), mesh, u0.cpu().numpy(), dt, 50, ours50, device)
+        del ours50
     line = {"metric": "DOF*steps/s (3D Burgers 256^3 x 3 channels, SETDRK4, FP32)", "value": dof_steps / (ms * 1e-3),
             "unit": "DOF*steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/c64",
             "data": "synthetic (seeded GRF velocity)",
             "config": {"workload": "burgers3d_256cubed_200steps", "result_finite": finite,
-                       "l2": "inputs (200 MB state, 1.6 GB workspace) larger than L2"},
+                       "l2": "inputs (200 MB state, 1.6 GB workspace) larger than L2",
+                       "rel_l2_vs_fp64_after_50_steps": (fp64 or {}).get("rel_l2")},
+            "accuracy_vs_fp64": fp64,
             "gpu_launches": plan.launch_count(steps, 1) * args.steps,
             "roofline": {"bound": "hbm", "per_kernel_ms": {k: v["avg_ms"] for k, v in prof.items() if v["launches"]},
                          "step_model_bytes_per_dof_step": 276,
@@ -804,6 +850,8 @@ def main():
     ap.add_argument("--cpu-time-steps", type=int, default=5)
     ap.add_argument("--no-torch-reference", action="store_true",
                     help="skip the reference torch GPU path leg of the ns2d workload")
+    ap.add_argument("--no-fp64-reference", action="store_true",
+                    help="skip the accuracy leg (the reference's float64 run of the first samples)")
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
     ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
@@ -885,7 +933,9 @@ def main():
         "config": {"workload": WORKLOAD, "grid": [N, N], "batch_per_gpu": res["B"], "time_steps": TIME_STEPS,
                    "dt": DT, "nu": 1.0 / RE, "integrator": "SETDRK4 (M=16, r=1)",
                    "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between timed steps",
-                   "result_finite": res["finite"]},
+                   "result_finite": res["finite"],
+                   "rel_l2_vs_fp64": (res["fp64"] or {}).get("rel_l2")},
+        "accuracy_vs_fp64": res["fp64"],
         "e2e": {"value": e2e_value, "unit": "DOF*steps/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"], "ms_per_step": res["e2e_ms"]},
         "gpu_launches": res["launches"] * args.steps,

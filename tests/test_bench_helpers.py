@@ -12,3 +12,49 @@ def test_fft_flop_fraction_of_the_1d_solve():
     assert math.isclose(r["achieved_tflops"], 210 * 128 * 200 / 1e-3 / 1e12)
     assert math.isclose(r["peak_tflops"], 152 * 128 * 2 * 2.07e3 / 1e6)
     assert math.isclose(r["frac"], r["achieved_tflops"] / r["peak_tflops"])
+
+
+def test_fp64_accuracy_leg_runs_the_reference_in_float64():
+    """The accuracy leg of the headline line integrates with the reference itself in float64: on the
+    CPU, at 32^2, its result equals the oracle's FP64 integration of the same vorticity to 1e-10, and an
+    FP32 run of the same reference lands inside the 1e-5 parity bar but not at FP64 round-off."""
+    import numpy as np
+    import pytest
+    import torch
+
+    R, why = bench._import_reference()
+    if R is None:
+        pytest.skip(why)
+    from oracle import spectral as S
+    from torchfsm_gb300 import initial
+
+    mesh = [(0.0, 2 * math.pi, 32)] * 2
+    w0 = initial.gaussian_random_field((32, 32), 2, 1, initial.vorticity_spectrum, 5)
+    w0 = w0 if w0.ndim == 4 else w0[:, None]
+    steps, dt = 20, 1e-3
+    ref64, _ = S.integrate(w0, mesh, [(1e-3, ("laplacian",))], [(-1.0, "vorticity_convection")], dt, steps)
+
+    def make(R):
+        return R.pde.NavierStokesVorticity(1000.0)
+
+    r = bench.fp64_reference_rel_l2(make, mesh, w0, dt, steps, ref64, "cpu")
+    assert r["samples"] == 2 and r["steps"] == steps
+    assert r["rel_l2"] < 1e-10, r
+    ours32 = make(R).integrate(u_0=torch.tensor(w0, dtype=torch.float32), mesh=mesh, dt=dt, step=steps)
+    r32 = bench.fp64_reference_rel_l2(make, mesh, w0, dt, steps, ours32, "cpu")
+    assert 1e-9 < r32["rel_l2"] < 1e-5, r32
+
+
+def test_fp64_accuracy_leg_reports_failure_instead_of_raising():
+    import numpy as np
+    import pytest
+
+    R, why = bench._import_reference()
+    if R is None:
+        pytest.skip(why)
+
+    def broken(R):
+        raise RuntimeError("no such operator")
+
+    r = bench.fp64_reference_rel_l2(broken, [(0.0, 1.0, 8)], np.zeros((1, 1, 8)), 0.1, 1, np.zeros((1, 1, 8)), "cpu")
+    assert "unavailable" in r and "no such operator" in r["unavailable"]

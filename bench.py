@@ -165,8 +165,7 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
     import __graft_entry__ as entry
 
     entry.build()
-    from torchfsm_gb300 import _lib, _native, pde
-    from torchfsm_gb300.mesh import FourierMesh
+    from torchfsm_gb300 import pde
 
     device = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(device)

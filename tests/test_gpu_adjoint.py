@@ -7,7 +7,6 @@ import pytest
 import torch
 
 import cases as C
-from torchfsm_gb300 import pde
 from torchfsm_gb300.operator import Convection, Laplacian
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")

@@ -1,6 +1,5 @@
 """Coefficient tables built on the GPU (FP64, rounded to FP32) against the reference's FP64 tables."""
 
-import math
 import os
 
 import numpy as np

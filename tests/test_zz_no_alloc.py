@@ -15,7 +15,6 @@ passes alone in a fresh process as well as after the other tests.
 import ctypes
 import math
 
-import numpy as np
 import pytest
 import torch
 

@@ -38,7 +38,6 @@ from __future__ import annotations
 
 import ctypes
 import math
-from typing import List, Optional, Sequence, Tuple
 
 import torch
 

@@ -4,8 +4,6 @@ The fused integrate path evaluates these in the CUDA kernels; the torch
 bodies here serve one-shot ``Operator.__call__``.
 """
 
-from typing import Optional
-
 from ...mesh import FourierMesh
 from .._base import CoreGenerator, NonlinearFunc, NonlinearOperator
 

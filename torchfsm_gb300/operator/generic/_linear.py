@@ -7,7 +7,7 @@ _spatial_derivative.py:7-20 and _source.py:9-17 of the reference.
 import torch
 
 from ...mesh import FourierMesh
-from .._base import CoreGenerator, LinearCoef, LinearOperator, Operator
+from .._base import CoreGenerator, LinearCoef, LinearOperator
 
 
 class _LaplacianCore(LinearCoef):

@@ -643,12 +643,16 @@ def run_serving(args):
     serve_tp = total / wall
     burst_lat = [r.t_done - r.arrival for r in reqs]
     # the plain drop-in, one solve at a time, same requests in the same order
-    alone_t, max_err = [], 0.0
+    alone_t, max_err, nonfinite_plain = [], 0.0, []
     for r in reqs:
         res, t = serving.solve_alone(r, device, ops)
         alone_t.append(t)
+        if not bool(torch.isfinite(res).all()):
+            nonfinite_plain.append(r.rid)
+            continue
         ref = res.double()
         max_err = max(max_err, float((r.result.double() - ref).norm() / max(ref.norm(), 1e-30)))
+    nonfinite_serve = [r.rid for r in reqs if r.finite is False]
     plain_tp = total / sum(alone_t)
     # Poisson arrivals at rates below the server's measured capacity: latency of each request
     # against its own one-at-a-time time (the streams hold the same requests at every rate)
@@ -682,7 +686,9 @@ def run_serving(args):
                         "isolated_latency_s": {"p50": _pctl(alone_t, 50), "p99": _pctl(alone_t, 99)},
                         "latency_over_isolated": {"p50": _pctl(ratio, 50), "p99": _pctl(ratio, 99)},
                         "poisson_sweep": sweep, "graph_replays": server.graph_replays,
-                        "max_rel_diff_mix_vs_alone": max_err},
+                        "max_rel_diff_mix_vs_alone": max_err,
+                        "nonfinite_requests": {"serve": len(nonfinite_serve), "plain": len(nonfinite_plain),
+                                               "same_requests": nonfinite_serve == nonfinite_plain}},
             "gpu_launches": server.launches,
             "e2e": {"value": serve_tp, "unit": "DOF*steps/s",
                     "h2d_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs),

@@ -26,3 +26,20 @@ def test_stream_mix_covers_both_kinds_and_ranges():
     assert {("ks1d", n) for n in (256, 512, 1024, 2048, 4096)} <= kinds
     assert {("burgers2d", n) for n in (64, 128, 256)} <= kinds
     assert all(1 <= r.batch <= 32 and 100 <= r.steps <= 2000 and 0.01 <= r.dt <= 0.1 for r in reqs)
+
+
+def test_request_reports_a_diverged_result():
+    import torch
+
+    from torchfsm_gb300.serving import SolveRequest
+
+    r = SolveRequest(0, "ks1d", 8, 1, 10, 0.1, torch.zeros(1, 1, 8))
+    assert r.finite is None  # no result yet
+    r.result = torch.ones(1, 1, 8)
+    assert r.finite is None  # copy to the host not yet complete
+    r.t_done = 1.0
+    assert r.finite is True
+    r.result[0, 0, 3] = float("nan")
+    assert r.finite is False
+    r.result[0, 0, 3] = float("inf")
+    assert r.finite is False

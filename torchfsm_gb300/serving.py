@@ -61,6 +61,14 @@ class SolveRequest:
     def dof_steps(self) -> int:
         return int(np.prod(self.u0.shape)) * self.steps
 
+    @property
+    def finite(self) -> Optional[bool]:
+        """False when the result holds NaN or Inf (the solve diverged), None before the result has
+        reached the host. Read it once ``t_done`` is set: the result is copied asynchronously."""
+        if self.result is None or self.t_done is None:
+            return None
+        return bool(torch.isfinite(self.result).all())
+
 
 def problem(kind: str, n: int):
     """(operator, mesh_info, channels) of a request kind."""

@@ -245,6 +245,62 @@ CASES.update({
 })
 
 
+def _allen_cahn_source(u):
+    return u - u ** 3
+
+
+def _damping_source(u):
+    return -0.5 * u * u.abs()
+
+
+def _burgers_with_sources(M):
+    x = M.torch.arange(64, dtype=M.torch.float64) / 64
+    forcing = (0.1 * M.torch.sin(2 * math.pi * x)).reshape(1, 1, 64)
+    return M.pde.Burgers(0.02) + M.operator.ImplicitSource(_damping_source) + forcing
+
+
+# Programs without a fused kernel (Python-callable sources, the conservative convection form, two
+# kinds of nonlinear term with an explicit source): integrate steps them through the cores'
+# Python callables with the library's coefficient tables and transforms.
+CALLBACK_CASES = {
+    "allencahn1d_n64": dict(
+        mesh=[(0, TWO_PI, 64)], batch=2, channels=1, dt=0.01, step=100, record=20,
+        build=lambda M: 0.05 * M.operator.Laplacian() + M.operator.ImplicitSource(_allen_cahn_source),
+        ic=_bl(231, (64,), 4, 0.5),
+    ),
+    "allencahn1d_setdrk2": dict(
+        mesh=[(0, TWO_PI, 64)], batch=2, channels=1, dt=0.01, step=50, record=0, integrator="setdrk2",
+        build=lambda M: 0.05 * M.operator.Laplacian() + M.operator.ImplicitSource(_allen_cahn_source),
+        ic=_bl(232, (64,), 4, 0.5),
+    ),
+    "allencahn1d_setdrk3_raw": dict(
+        mesh=[(0, TWO_PI, 64)], batch=1, channels=1, dt=0.01, step=50, record=0, integrator="setdrk3",
+        build=lambda M: 0.05 * M.operator.Laplacian()
+        + M.operator.ImplicitSource(_allen_cahn_source, non_linear=False),
+        ic=_bl(233, (64,), 4, 0.5),
+    ),
+    "allencahn1d_etdrk2": dict(
+        mesh=[(0, TWO_PI, 64)], batch=2, channels=1, dt=0.01, step=50, record=10, integrator="etdrk2",
+        build=lambda M: 0.05 * M.operator.Laplacian() + M.operator.ImplicitSource(_allen_cahn_source),
+        ic=_bl(234, (64,), 4, 0.5),
+    ),
+    "conservative_burgers2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=2, dt=0.01, step=30, record=10,
+        build=lambda M: 0.01 * M.operator.Laplacian() - M.operator.ConservativeConvection(),
+        ic=_bl(235, (32, 32), 4, 0.25),
+    ),
+    "burgers1d_sources_n64": dict(
+        mesh=[(0, 1, 64)], batch=2, channels=1, dt=0.005, step=60, record=15,
+        build=_burgers_with_sources,
+        ic=_bl(236, (64,), 4, 0.5),
+    ),
+}
+
+
+def _case(name: str) -> dict:
+    return CASES[name] if name in CASES else CALLBACK_CASES[name]
+
+
 def set_case_integrator(op, M, kind):
     """Select a case's integrator by name on a torchfsm-like namespace."""
     if kind in RK_NAMES:
@@ -256,12 +312,12 @@ def set_case_integrator(op, M, kind):
 
 
 def initial_condition(name: str) -> np.ndarray:
-    c = CASES[name]
+    c = _case(name)
     return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)
 
 
 def record_fn(name: str):
-    every = CASES[name]["record"]
+    every = _case(name)["record"]
     if not every:
         return None
     return lambda step: step % every == 0

@@ -5,9 +5,9 @@ Run in a container where the reference (torchfsm 0.0.4) is importable:
     python tests/golden/make_golden.py /root/reference
 
 The reference is imported from the given source tree and run on the CPU in
-float64 for every case of ``cases.py``; the initial condition, the final
-physical state and (where recorded) the physical trajectory are stored in
-``<case>.npz``. ``phi_coefs.npz`` holds the reference's SETDRK4 / ETDRK
+float64 for every case of ``cases.py`` (``CASES`` and ``CALLBACK_CASES``); the
+initial condition, the final physical state and (where recorded) the physical
+trajectory are stored in ``<case>.npz``. ``phi_coefs.npz`` holds the reference's SETDRK4 / ETDRK
 coefficient tables for a few linear symbols and ``masks.npz`` its 2/3 dealias
 masks. These files are the pins of the numpy oracle and of the GPU path; the
 GPU tests never read the reference itself.
@@ -41,7 +41,7 @@ def main(ref_root: str) -> None:
 
     M = C.namespace("torchfsm")
     only = set(sys.argv[2:])
-    for name, case in C.CASES.items():
+    for name, case in list(C.CASES.items()) + list(C.CALLBACK_CASES.items()):
         if only and name not in only:
             continue
         u0 = C.initial_condition(name)

@@ -53,9 +53,10 @@ def test_deterministic():
     assert torch.equal(a, b)
 
 
-def test_python_callable_source_is_reported_unsupported():
+def test_python_callable_source_with_runge_kutta_is_reported_unsupported():
     M = C.namespace("torchfsm_gb300")
     op = M.operator.Laplacian() + M.operator.ImplicitSource(lambda u: u ** 2)
+    op.set_integrator(M.integrator.RKIntegrator.RK4)
     u0 = torch.rand(1, 1, 64, device="cuda")
     with pytest.raises(_lib.UnsupportedProgram):
         op.integrate(u_0=u0, mesh=[(0, 1, 64)], dt=0.01, step=2)

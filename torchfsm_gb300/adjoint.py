@@ -313,6 +313,9 @@ def _prepare_and_apply(op, u0, dt, steps, checkpoint):
         op._build_integrator(dt, u0.device)
         integ = op._state_dict["integrator"]
     plan = integ.plan
+    if not isinstance(plan, _native.NativePlan):
+        raise NotImplementedError("gradients are provided for programs the fused kernels run "
+                                  "(not for nonlinear terms stepped through Python callables)")
     prog = plan.program
     if plan.integrator != _lib.FSM_SETDRK4:
         raise NotImplementedError("gradients are provided for the SETDRK4 integrator")

@@ -20,6 +20,7 @@ from torch import Tensor
 
 from .. import _lib, _native
 from ..integrator import ETDRKIntegrator, RKIntegrator, SETDRKIntegrator
+from ..integrator._callback import CALLBACK_SCHEMES, CallbackPlan
 from ..mesh import FourierMesh, MeshGrid
 from ..traj_recorder import _TrajRecorder
 from ..utils import default
@@ -338,8 +339,25 @@ class OperatorLike(_MutableMixIn):
         if integ == _lib.FSM_ETDRK0:
             assert self.is_linear, "The ETDRK0 integrator only supports linear term"
         f_mesh = self._state_dict["f_mesh"]
-        prog = _native.lower(self._linear_terms, self._nonlinear_funcs, f_mesh, self._state_dict["n_channel"],
-                             self._de_aliasing_rate)
+        callback = False
+        try:
+            prog = _native.lower(self._linear_terms, self._nonlinear_funcs, f_mesh, self._state_dict["n_channel"],
+                                 self._de_aliasing_rate)
+        except _lib.UnsupportedProgram as err:
+            # nonlinear terms without a fused kernel: the linear part's plan steps them through the
+            # cores' Python callables (integrator/_callback.py); anything else stays unsupported
+            if not self._nonlinear_funcs:
+                raise
+            try:
+                prog = _native.lower(self._linear_terms, [], f_mesh, self._state_dict["n_channel"],
+                                     self._de_aliasing_rate)
+            except _lib.UnsupportedProgram:
+                raise err from None
+            if integ not in CALLBACK_SCHEMES:
+                raise _lib.UnsupportedProgram(
+                    _lib.FSM_ERR_UNSUPPORTED,
+                    f"{err}; such terms step with ETDRK1/2 or SETDRK1-4, not the Runge-Kutta schemes") from None
+            callback = True
         cfg = dict(self._integrator_config)
         try:
             plan = _native.NativePlan(
@@ -355,6 +373,8 @@ class OperatorLike(_MutableMixIn):
                     f"Original error message: {e}",
                     "Please try to use a smaller mesh or a low-order integrator."])) from e
             raise
+        if callback:
+            plan = CallbackPlan(plan, self._nonlinear_funcs, f_mesh, self._de_aliasing_rate)
         self._is_etdrk_integrator = True
         self._state_dict["integrator"] = NativeETDIntegrator(plan)
 

@@ -10,7 +10,7 @@ from ._linear import _ImplicitUnitSourceCore
 
 
 class _ImplicitFuncSourceCore(NonlinearFunc):
-    """fft(f(u)) of a Python callable f; no fused kernel (integrate raises UnsupportedProgram)."""
+    """fft(f(u)) of a Python callable f; no fused kernel: integrate steps it through the callable."""
 
     def __init__(self, source_func: Callable[[torch.Tensor], torch.Tensor], non_linear: bool = True) -> None:
         super().__init__(non_linear)

@@ -377,6 +377,45 @@ def fp64_reference_rel_l2(make_op, mesh, u0: np.ndarray, dt: float, steps: int, 
         return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
+def reference_request_sample(reqs, device, count: int) -> dict:
+    """The reference's own ``integrate`` (baseline/_ref, its public API and stock code path) on a
+    bounded sample of a serving stream: the ``count`` cheapest requests by DOF*steps, solved one at
+    a time on ``device`` (cuda: the reference's torch GPU path; cpu: its CPU path on the host
+    cores), each timed from the host field to the host result. Reports DOF*steps/s over the sample
+    and, for requests that hold our served result, the largest rel-L2 distance of ours from the
+    reference's FP32 result per request kind."""
+    import torch
+
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    from torchfsm_gb300 import serving
+
+    device = torch.device(device)
+    sample = sorted(reqs, key=lambda r: (r.dof_steps, r.rid))[:count]
+    ops, total, secs, diffs = {}, 0, 0.0, {}
+    for r in sample:
+        key = (r.kind, r.n)
+        if key not in ops:
+            ref_op = R.pde.KuramotoSivashinsky() if r.kind == "ks1d" else R.pde.Burgers(serving.BURGERS_NU)
+            ops[key] = (ref_op, serving.problem(r.kind, r.n)[1])
+        ref_op, mesh = ops[key]
+        if device.type == "cuda":
+            torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        out = ref_op.integrate(u_0=r.u0.to(device), mesh=mesh, dt=r.dt, step=r.steps).cpu()
+        secs += time.perf_counter() - t0
+        total += r.dof_steps
+        if r.result is not None:
+            d = float((r.result.double() - out.double()).norm() / max(float(out.double().norm()), 1e-30))
+            diffs[r.kind] = max(diffs.get(r.kind, 0.0), d)
+    return {"value": total / secs if secs > 0 else None, "unit": "DOF*steps/s", "requests": len(sample),
+            "rids": [r.rid for r in sample], "seconds": secs, "device": str(device),
+            "cores": torch.get_num_threads() if device.type == "cpu" else None,
+            "max_rel_l2_served_vs_reference_fp32": diffs,
+            "kind": f"reference integrate, one request at a time, on {device.type}"}
+
+
 def profile_kernels(plan, state0, ws, device) -> dict:
     """Average device time of each kernel kind over one instrumented integration."""
     import torch
@@ -653,6 +692,17 @@ def run_serving(args):
         ref = res.double()
         max_err = max(max_err, float((r.result.double() - ref).norm() / max(ref.norm(), 1e-30)))
     nonfinite_serve = [r.rid for r in reqs if r.finite is False]
+    # the reference's own path on bounded samples of the same stream (cheapest requests first),
+    # beside our one-at-a-time path on the same requests
+    alone_by_rid = {r.rid: t for r, t in zip(reqs, alone_t)}
+    reference_sample = {}
+    for leg, dev, cnt in (("torch_gpu", device, args.ref_requests), ("cpu", "cpu", args.ref_cpu_requests)):
+        res = reference_request_sample(reqs, dev, cnt)
+        if "rids" in res:
+            ours_s = sum(alone_by_rid[i] for i in res["rids"])
+            dof = sum(r.dof_steps for r in reqs if r.rid in set(res["rids"]))
+            res["plain_value_same_requests"] = dof / ours_s if ours_s > 0 else None
+        reference_sample[leg] = res
     plain_tp = total / sum(alone_t)
     # Poisson arrivals at rates below the server's measured capacity: latency of each request
     # against its own one-at-a-time time (the streams hold the same requests at every rate)
@@ -688,7 +738,8 @@ def run_serving(args):
                         "poisson_sweep": sweep, "graph_replays": server.graph_replays,
                         "max_rel_diff_mix_vs_alone": max_err,
                         "nonfinite_requests": {"serve": len(nonfinite_serve), "plain": len(nonfinite_plain),
-                                               "same_requests": nonfinite_serve == nonfinite_plain}},
+                                               "same_requests": nonfinite_serve == nonfinite_plain},
+                        "reference_sample": reference_sample},
             "gpu_launches": server.launches,
             "e2e": {"value": serve_tp, "unit": "DOF*steps/s",
                     "h2d_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs),
@@ -871,6 +922,10 @@ def main():
                     help="skip the accuracy leg (the reference's float64 run of the first samples)")
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
+    ap.add_argument("--ref-requests", type=int, default=20,
+                    help="serving: requests of the stream run by the reference's torch GPU path")
+    ap.add_argument("--ref-cpu-requests", type=int, default=3,
+                    help="serving: requests of the stream run by the reference's CPU path")
     ap.add_argument("--load", type=float, default=0.7, help="serving: Poisson rate as a fraction of capacity")
     ap.add_argument("--threaded", type=int, default=1, help="serving: one host worker thread per bucket")
     ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],

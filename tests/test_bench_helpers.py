@@ -58,3 +58,26 @@ def test_fp64_accuracy_leg_reports_failure_instead_of_raising():
 
     r = bench.fp64_reference_rel_l2(broken, [(0.0, 1.0, 8)], np.zeros((1, 1, 8)), 0.1, 1, np.zeros((1, 1, 8)), "cpu")
     assert "unavailable" in r and "no such operator" in r["unavailable"]
+
+
+def test_reference_request_sample_runs_the_reference_on_the_cheapest_requests():
+    import numpy as np
+    import pytest
+    import torch
+
+    R, why = bench._import_reference()
+    if R is None:
+        pytest.skip(why)
+    from torchfsm_gb300.serving import SolveRequest
+
+    rng = np.random.default_rng(3)
+    reqs = [
+        SolveRequest(0, "ks1d", 256, 1, 6, 0.05, torch.tensor(rng.standard_normal((1, 1, 256)), dtype=torch.float32)),
+        SolveRequest(1, "burgers2d", 64, 1, 3, 0.02,
+                     torch.tensor(0.25 * rng.standard_normal((1, 2, 64, 64)), dtype=torch.float32)),
+        SolveRequest(2, "ks1d", 512, 2, 50, 0.05, torch.zeros(2, 1, 512)),
+    ]
+    r = bench.reference_request_sample(reqs, "cpu", 2)
+    assert r["requests"] == 2 and sorted(r["rids"]) == [0, 1]  # the two cheapest
+    assert r["value"] > 0 and r["unit"] == "DOF*steps/s"
+    assert r["max_rel_l2_served_vs_reference_fp32"] == {}  # no served results yet

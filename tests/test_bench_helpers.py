@@ -81,3 +81,20 @@ def test_reference_request_sample_runs_the_reference_on_the_cheapest_requests():
     assert r["requests"] == 2 and sorted(r["rids"]) == [0, 1]  # the two cheapest
     assert r["value"] > 0 and r["unit"] == "DOF*steps/s"
     assert r["max_rel_l2_served_vs_reference_fp32"] == {}  # no served results yet
+
+
+def test_energy_spectrum_of_single_modes():
+    import torch
+
+    n = 32
+    x = torch.arange(n, dtype=torch.float64) / n * 2 * math.pi
+    u = (torch.cos(3 * x) + 2 * torch.sin(5 * x)).reshape(1, 1, n)
+    e = bench.energy_spectrum(u)
+    # |u_hat(+-k)| = n a / 2 for amplitude a: shell k holds a^2 / 2
+    assert math.isclose(float(e[3]), 0.5, rel_tol=1e-12) and math.isclose(float(e[5]), 2.0, rel_tol=1e-12)
+    assert float(e.sum()) == float(e[3] + e[5])
+    # Parseval: the shells sum to the mean square of the field
+    assert math.isclose(float(e.sum()), float((u ** 2).mean()), rel_tol=1e-12)
+    v = torch.cos(x.reshape(n, 1) + 2 * x.reshape(1, n)).reshape(1, 1, n, n).repeat(2, 2, 1, 1)
+    e2 = bench.energy_spectrum(v)  # |k| = sqrt(5) -> shell 2, two channels
+    assert math.isclose(float(e2[2]), 1.0, rel_tol=1e-12) and math.isclose(float(e2.sum()), 1.0, rel_tol=1e-12)

@@ -1023,8 +1023,9 @@ def main():
     peak, peak_kind = _peaks()
     col = res["prof"]["column_pass"]
     achieved = column_pass_bytes(res["B"]) / (col["avg_ms"] * 1e-3) / 1e9 if col["avg_ms"] else None
+    # the CPU baseline is timed at N = 1 only (the host cores are shared by all ranks otherwise)
     cpu = cpu_reference_throughput(min(BATCH, max(os.cpu_count() or 1, args.cpu_samples)), args.cpu_time_steps,
-                                   os.cpu_count() or 1)
+                                   os.cpu_count() or 1) if world == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": "DOF*steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
@@ -1048,7 +1049,7 @@ def main():
                      "per_kernel_ms": {k: v["avg_ms"] for k, v in res["prof"].items() if v["launches"]},
                      "step_model_bytes_per_dof_step": 212,
                      "step_achieved_gbs": 212.0 * dof_steps / world / (res["ms"] * 1e-3) / 1e9 * world},
-        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
         "torch_gpu_reference": res["torch_ref"],
         "clocks": res["clocks"],
     }

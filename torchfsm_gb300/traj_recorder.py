@@ -158,7 +158,10 @@ class DiskRecorder(_TrajRecorder):
     The reference's chunk test is broken (``len(self.traj<...)``); this one
     buffers ``cache_freq`` frames, then stacks them to [B, T, C, ..], converts
     them to physical space unless ``return_in_fourier`` and saves
-    ``temp_cache_{step}`` with torch.save or np.save. ``trajectory`` is None.
+    ``temp_cache_{step}`` (``step`` = the chunk's last recorded step) with
+    torch.save or np.save (``.npy``). Reading ``trajectory`` -- ``integrate``
+    does so after the last step -- saves the frames still buffered as a last,
+    shorter chunk and returns None.
     """
 
     def __init__(self, control_func=None, include_initial_state: bool = True, cache_dir: Optional[str] = None,
@@ -174,10 +177,12 @@ class DiskRecorder(_TrajRecorder):
         self.temp_cache_loc = temp_cache_loc
         self.save_format = save_format
         self._trajectory: List[torch.Tensor] = []
+        self._last_step = 0
 
     def _record(self, step: int, frame: torch.Tensor):
         keep = frame.cpu() if (self.temp_cache_loc == "cpu" and not frame.is_cpu) else frame.clone()
         self._trajectory.append(keep)
+        self._last_step = step
         if len(self._trajectory) >= self.cache_freq:
             self._flush(step)
 
@@ -198,6 +203,8 @@ class DiskRecorder(_TrajRecorder):
 
     @property
     def trajectory(self):
+        if self._trajectory:
+            self._flush(self._last_step)
         return None
 
 

@@ -84,3 +84,19 @@ def test_linear_part_that_changes_channels_stays_unsupported(cpu_library):
     op = M.operator.Grad() + M.operator.ImplicitSource(lambda u: u ** 2)
     with pytest.raises((_lib.UnsupportedProgram, ValueError)):
         op.integrate(u_0=torch.rand(1, 1, 16, 16), mesh=[(0, 1, 16), (0, 1, 16)], dt=0.01, step=1)
+
+
+def test_batched_linear_coefficient_matches_samples_run_alone(cpu_library):
+    """A tensor coefficient [B, 1, 1] on the linear term gives one table entry per sample."""
+    M = C.namespace("torchfsm_gb300")
+    u0 = torch.tensor(C.initial_condition("allencahn1d_n64"), dtype=torch.float32)
+    mesh = [(0, 2 * np.pi, 64)]
+    nus = torch.tensor([0.05, 0.2], dtype=torch.float32).reshape(2, 1, 1)
+    op = nus * M.operator.Laplacian() + M.operator.ImplicitSource(C._allen_cahn_source)
+    both = op.integrate(u_0=u0, mesh=mesh, dt=0.01, step=40)
+    plan = op._state_dict["integrator"].plan
+    assert plan.tables.shape[1] == 2  # lin_batch
+    for b in range(2):
+        alone_op = float(nus[b]) * M.operator.Laplacian() + M.operator.ImplicitSource(C._allen_cahn_source)
+        alone = alone_op.integrate(u_0=u0[b : b + 1], mesh=mesh, dt=0.01, step=40)
+        assert S.rel_l2(both[b : b + 1].numpy(), alone.numpy()) <= 1e-6

@@ -16,6 +16,11 @@ field, E(k) ~ k^4 exp(-(k/4)^2), zero mean, unit RMS).
   cpu_baseline / --impl reference : the numpy restatement of the reference's
              algorithm (oracle/spectral.py) in complex64 on all host cores, on a
              bounded sample of the same workload.
+  torch_gpu_reference / reference_cpu : the reference package itself (installed
+             under baseline/_ref) on the same GPU, and on the host cores on a
+             bounded sample of the batch.
+  accuracy_vs_fp64 : the first samples of our result against the reference's
+             own integrator run in float64 on the GPU, all 1000 steps.
 
 Under torchrun every rank integrates its own batch of 64 (replicas, weak
 scaling, no collective on the data path); the time is the max over ranks.
@@ -344,6 +349,41 @@ def torch_gpu_reference(device, w0: np.ndarray, ours_half=None, k1: int = 10, k2
         res["rel_l2_vs_fused_after_%d_steps" % k1] = float(
             torch.linalg.vector_norm(ours - out1) / torch.linalg.vector_norm(out1))
     return res
+
+
+def reference_cpu_throughput(samples: int, k1: int = 1, k2: int = 4, threads: int = 0) -> dict:
+    """The reference's own path on the host cores: the unmodified package under baseline/_ref,
+    ``NavierStokesVorticity(1000).integrate`` on a CPU mesh in float32 (torch CPU FFTs and
+    elementwise kernels, all host threads), on a bounded sample of the workload: ``samples`` of
+    the 64 seeded fields. Each integrate call carries the reference's fixed gc/empty_cache cost,
+    so the steady time per step is the difference of a k2-step and a k1-step call."""
+    import torch
+
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    threads = threads or os.cpu_count() or 1
+    prev = torch.get_num_threads()
+    torch.set_num_threads(threads)
+    try:
+        u = torch.tensor(initial_vorticity(samples, seed=SEED))
+        u = u if u.dim() == 4 else u.unsqueeze(1)
+        op = R.pde.NavierStokesVorticity(RE)
+        op.integrate(u_0=u, mesh=MESH, dt=DT, step=1)  # registers the mesh, builds the coefficients
+
+        def timed(k):
+            t0 = time.perf_counter()
+            op.integrate(u_0=u, dt=DT, step=k)
+            return time.perf_counter() - t0
+
+        t1, t2 = timed(k1), timed(k2)
+        per_step = max(t2 - t1, 1e-9) / (k2 - k1)
+    finally:
+        torch.set_num_threads(prev)
+    return {"value": samples * N * N / per_step, "unit": "DOF*steps/s", "ms_per_step": per_step * 1e3,
+            "cores": threads, "kind": "reference package on the host cores (torch CPU), FP32",
+            "sample": f"{samples} samples of the 256^2 batch, steady step from a {k2}- and a {k1}-step call",
+            "call_s": [t1, t2], "version": getattr(R, "__version__", "0.0.4")}
 
 
 def fp64_reference_rel_l2(make_op, mesh, u0: np.ndarray, dt: float, steps: int, ours, device) -> dict:
@@ -945,6 +985,8 @@ def main():
     ap.add_argument("--cpu-time-steps", type=int, default=5)
     ap.add_argument("--no-torch-reference", action="store_true",
                     help="skip the reference torch GPU path leg of the ns2d workload")
+    ap.add_argument("--ref-cpu-samples", type=int, default=8,
+                    help="ns2d: samples of the batch run by the reference package on the host cores (0: skip)")
     ap.add_argument("--no-fp64-reference", action="store_true",
                     help="skip the accuracy leg (the reference's float64 run of the first samples)")
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
@@ -1023,9 +1065,10 @@ def main():
     peak, peak_kind = _peaks()
     col = res["prof"]["column_pass"]
     achieved = column_pass_bytes(res["B"]) / (col["avg_ms"] * 1e-3) / 1e9 if col["avg_ms"] else None
-    # the CPU baseline is timed at N = 1 only (the host cores are shared by all ranks otherwise)
+    # the CPU baselines are timed at N = 1 only (the host cores are shared by all ranks otherwise)
     cpu = cpu_reference_throughput(min(BATCH, max(os.cpu_count() or 1, args.cpu_samples)), args.cpu_time_steps,
                                    os.cpu_count() or 1) if world == 1 else None
+    ref_cpu = reference_cpu_throughput(args.ref_cpu_samples) if world == 1 and args.ref_cpu_samples > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": "DOF*steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
@@ -1051,12 +1094,15 @@ def main():
                      "step_achieved_gbs": 212.0 * dof_steps / world / (res["ms"] * 1e-3) / 1e9 * world},
         "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
         "torch_gpu_reference": res["torch_ref"],
+        "reference_cpu": ref_cpu,
         "clocks": res["clocks"],
     }
     tr = res["torch_ref"]
     if tr and "value" in tr:
         tr["fused_device_over_reference"] = value / tr["value"]
         tr["fused_e2e_over_reference"] = e2e_value / tr["value"]
+    if ref_cpu and "value" in ref_cpu:
+        ref_cpu["fused_e2e_over_reference_cpu"] = e2e_value / ref_cpu["value"]
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

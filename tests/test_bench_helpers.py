@@ -98,3 +98,14 @@ def test_energy_spectrum_of_single_modes():
     v = torch.cos(x.reshape(n, 1) + 2 * x.reshape(1, n)).reshape(1, 1, n, n).repeat(2, 2, 1, 1)
     e2 = bench.energy_spectrum(v)  # |k| = sqrt(5) -> shell 2, two channels
     assert math.isclose(float(e2[2]), 1.0, rel_tol=1e-12) and math.isclose(float(e2.sum()), 1.0, rel_tol=1e-12)
+
+
+def test_reference_cpu_leg_times_the_reference_package():
+    import pytest
+
+    R, why = bench._import_reference()
+    if R is None:
+        pytest.skip(why)
+    r = bench.reference_cpu_throughput(1, k1=1, k2=2, threads=2)
+    assert r["value"] > 0 and r["cores"] == 2 and r["unit"] == "DOF*steps/s"
+    assert "torch CPU" in r["kind"]

@@ -459,9 +459,17 @@ def reference_request_sample(reqs, device, count: int) -> dict:
     R, why = _import_reference()
     if R is None:
         return {"unavailable": why}
+    try:
+        return _reference_request_sample(R, reqs, torch.device(device), count)
+    except Exception as e:  # noqa: BLE001 -- a baseline leg must not cost the serving line
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def _reference_request_sample(R, reqs, device, count: int) -> dict:
+    import torch
+
     from torchfsm_gb300 import serving
 
-    device = torch.device(device)
     sample = sorted(reqs, key=lambda r: (r.dof_steps, r.rid))[:count]
     ops, total, secs, diffs, spec_diffs = {}, 0, 0.0, {}, {}
     for r in sample:

@@ -1,8 +1,10 @@
 """Vector-calculus cores: Grad, Div, Curl (operator/generic/_grad.py, _div.py, _curl.py).
 
-They change the channel count (scalar -> vector, vector -> scalar), so they serve one-shot
-``Operator.__call__`` / ``functional`` evaluation (post-processing) with torch spectral
-multiplies on the input's device; ``integrate`` reports them unsupported.
+They serve one-shot ``Operator.__call__`` / ``functional`` evaluation (post-processing) with
+torch spectral multiplies on the input's device. ``integrate`` of Grad (a linear term that
+changes the channel count) reports it unsupported; Div and Curl are nonlinear terms without a
+fused kernel, so ``integrate`` steps them through the callback path, where their values
+broadcast against the state as in the reference's stage arithmetic.
 """
 
 import torch

@@ -5,7 +5,8 @@
 * ``_native.NativePlan`` by a plan of a linear part whose coefficient tables are the oracle's
   FP64 tables of the same linear symbol, laid out as the library lays them out
   (``fsm_plan_tables``: [tables][lin_batch][lin_channel][half spectrum], per scheme E, E2,
-  c1.. in the library's order);
+  c1.. in the library's order), and which steps linear ETDRK0 programs as the pointwise
+  kernel does (every point times E per step);
 * ``_native.Spectral``'s forward and inverse transforms by torch's real FFTs;
 * the CUDA-input check by a no-op,
 
@@ -25,9 +26,10 @@ _RealSpectral = _native.Spectral
 
 def _library_tables(integrator: int, lin: np.ndarray, dt: float, m: int, r: float) -> list:
     """The scheme's tables in the library's order (oracle values, FP64)."""
-    if integrator in (_lib.FSM_ETDRK1, _lib.FSM_ETDRK2):
-        t = S.etdrk_coefs(1 if integrator == _lib.FSM_ETDRK1 else 2, lin, dt)
-        keys = ["E", "c1"] + (["c2"] if integrator == _lib.FSM_ETDRK2 else [])
+    if integrator in (_lib.FSM_ETDRK0, _lib.FSM_ETDRK1, _lib.FSM_ETDRK2):
+        order = {_lib.FSM_ETDRK0: 0, _lib.FSM_ETDRK1: 1, _lib.FSM_ETDRK2: 2}[integrator]
+        t = S.etdrk_coefs(order, lin, dt)
+        keys = ["E", "c1", "c2"][: order + 1]
     else:
         order = {_lib.FSM_SETDRK1: 1, _lib.FSM_SETDRK2: 2, _lib.FSM_SETDRK3: 3, _lib.FSM_SETDRK4: 4}[integrator]
         t = S.setdrk_coefs(order, lin, dt, m, r)
@@ -61,8 +63,22 @@ class _CpuLinearPlan:
         self._tables = np.stack([t.reshape(-1) for t in _library_tables(
             integrator, lin, self.dt, n_integration_points, integration_radius)])
 
+        self._lin_shape = lin.shape
+
     def tables(self):
         return torch.from_numpy(self._tables.astype(np.complex64))
+
+    def integrate_half(self, state, steps, slots=None, traj=None, workspace=None):
+        """Linear programs (ETDRK0): every point advances by E per step, as the pointwise kernel."""
+        if self.integrator != _lib.FSM_ETDRK0:
+            raise NotImplementedError("the CPU stand-in steps linear ETDRK0 programs only")
+        E = self.tables()[0].reshape(self._lin_shape)
+        for i in range(steps):
+            if slots is not None and slots[i] >= 0:
+                traj[:, slots[i]] = state
+            state.mul_(E)
+        if slots is not None and slots[steps] >= 0:
+            traj[:, slots[steps]] = state
 
 
 class _CpuSpectral(_RealSpectral):

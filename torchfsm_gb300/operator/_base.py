@@ -386,7 +386,9 @@ class OperatorLike(_MutableMixIn):
         Returns the final field [B, C, n1..] (real, or the full complex
         spectrum if ``return_in_fourier``), or with a recorder its
         ``trajectory`` [B, T, C, n1..]. Runs in FP32/complex64 on the CUDA
-        device of the input.
+        device of the input. ``progressive`` (the reference's tqdm bar) is
+        accepted and has no effect: the steps are enqueued as one launch
+        sequence, with no per-step host loop to report on.
         """
         if self._state_dict["f_mesh"] is None or mesh is not None:
             mesh, n_channel = self._pre_check(u=u_0, u_fft=u_0_fft, mesh=mesh)

@@ -49,8 +49,8 @@ extern "C" {
 #define FSM_ERR_UNSUPPORTED 2  /* program or size without a fused kernel */
 #define FSM_ERR_CUDA 3         /* a CUDA call failed */
 #define FSM_ERR_OOM 4          /* device allocation failed */
-#define FSM_ERR_NONFINITE 5    /* a result holds NaN or Inf */
-#define FSM_ERR_TIMEOUT 6      /* a bounded device wait ran out */
+#define FSM_ERR_NONFINITE 5    /* a result holds NaN or Inf (reserved: fsm_nonfinite_flags reports it per field) */
+#define FSM_ERR_TIMEOUT 6      /* a bounded device wait ran out (reserved: no kernel here waits on a device flag) */
 
 /* nonlinear term of the program (at most one, plus an optional explicit source) */
 #define FSM_NL_NONE 0        /* linear, or explicit source only */

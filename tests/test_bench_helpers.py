@@ -109,3 +109,28 @@ def test_reference_cpu_leg_times_the_reference_package():
     r = bench.reference_cpu_throughput(1, k1=1, k2=2, threads=2)
     assert r["value"] > 0 and r["cores"] == 2 and r["unit"] == "DOF*steps/s"
     assert "torch CPU" in r["kind"]
+
+
+def test_reference_arm_prints_one_line_with_the_contract_keys():
+    import json
+    import os
+    import subprocess
+    import sys
+
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    cmd = [sys.executable, os.path.join(repo, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "0",
+           "--cpu-samples", "1", "--cpu-time-steps", "1"]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=600, cwd=repo)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["unit"] == "DOF*steps/s" and line["higher_is_better"] is True
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    # under torchrun only rank 0 runs and prints
+    env.update(RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=600, cwd=repo)
+    assert r.returncode == 0 and r.stdout.strip() == ""

@@ -38,6 +38,7 @@ import statistics
 import subprocess
 import sys
 import time
+from typing import Optional
 
 import numpy as np
 
@@ -991,6 +992,51 @@ def ncu_case(workload: str = "ns2d", n3d: int = 256):
     print("ncu case done", bool(torch.isfinite(out).all().item()))
 
 
+def fused_line(res: dict, args, world: int, cpu: Optional[dict], ref_cpu: Optional[dict]) -> dict:
+    """The JSON line of the fused arm from ``run_fused``'s measurements and the CPU baselines."""
+    dof_steps = res["B"] * N * N * TIME_STEPS
+    value = job_throughput(dof_steps, world, res["ms"])
+    e2e_value = job_throughput(dof_steps, world, res["e2e_ms"])
+    peak, peak_kind = _peaks()
+    col = res["prof"]["column_pass"]
+    achieved = column_pass_bytes(res["B"]) / (col["avg_ms"] * 1e-3) / 1e9 if col["avg_ms"] else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF*steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/c64", "data": "synthetic (seeded GRF vorticity)",
+        "config": {"workload": WORKLOAD, "grid": [N, N], "batch_per_gpu": res["B"], "time_steps": TIME_STEPS,
+                   "dt": DT, "nu": 1.0 / RE, "integrator": "SETDRK4 (M=16, r=1)",
+                   "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between timed steps",
+                   "result_finite": res["finite"],
+                   "rel_l2_vs_fp64": (res["fp64"] or {}).get("rel_l2")},
+        "accuracy_vs_fp64": res["fp64"],
+        "e2e": {"value": e2e_value, "unit": "DOF*steps/s", "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"], "ms_per_step": res["e2e_ms"],
+                "first_call_with_build_ms": res["first_ms"]},
+        "gpu_launches": res["launches"] * args.steps,
+        "roofline": {"bound": "hbm", "kernel": "k_axis0_r<256, VORTICITY, 2> (column pass)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": COLUMN_PASS_DRAM_BYTES,
+                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one stage-0 column pass "
+                                     "launch of this workload (bench.py --ncu-case)",
+                     "peak_source": f"{peak_kind} hbm_gbs",
+                     "per_kernel_ms": {k: v["avg_ms"] for k, v in res["prof"].items() if v["launches"]},
+                     "step_model_bytes_per_dof_step": 212,
+                     "step_achieved_gbs": 212.0 * dof_steps / world / (res["ms"] * 1e-3) / 1e9 * world},
+        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
+        "torch_gpu_reference": res["torch_ref"],
+        "reference_cpu": ref_cpu,
+        "clocks": res["clocks"],
+    }
+    tr = res["torch_ref"]
+    if tr and "value" in tr:
+        tr["fused_device_over_reference"] = value / tr["value"]
+        tr["fused_e2e_over_reference"] = e2e_value / tr["value"]
+    if ref_cpu and "value" in ref_cpu:
+        ref_cpu["fused_e2e_over_reference_cpu"] = e2e_value / ref_cpu["value"]
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1075,50 +1121,11 @@ def main():
         if dist is not None:
             dist.destroy_process_group()
         return
-    dof_steps = res["B"] * N * N * TIME_STEPS
-    value = job_throughput(dof_steps, world, res["ms"])
-    e2e_value = job_throughput(dof_steps, world, res["e2e_ms"])
-    peak, peak_kind = _peaks()
-    col = res["prof"]["column_pass"]
-    achieved = column_pass_bytes(res["B"]) / (col["avg_ms"] * 1e-3) / 1e9 if col["avg_ms"] else None
     # the CPU baselines are timed at N = 1 only (the host cores are shared by all ranks otherwise)
     cpu = cpu_reference_throughput(min(BATCH, max(os.cpu_count() or 1, args.cpu_samples)), args.cpu_time_steps,
                                    os.cpu_count() or 1) if world == 1 else None
     ref_cpu = reference_cpu_throughput(args.ref_cpu_samples) if world == 1 and args.ref_cpu_samples > 0 else None
-    line = {
-        "metric": METRIC, "value": value, "unit": "DOF*steps/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32/c64", "data": "synthetic (seeded GRF vorticity)",
-        "config": {"workload": WORKLOAD, "grid": [N, N], "batch_per_gpu": res["B"], "time_steps": TIME_STEPS,
-                   "dt": DT, "nu": 1.0 / RE, "integrator": "SETDRK4 (M=16, r=1)",
-                   "parallelism": f"replicas x{world}", "l2": "flushed (256 MB write) between timed steps",
-                   "result_finite": res["finite"],
-                   "rel_l2_vs_fp64": (res["fp64"] or {}).get("rel_l2")},
-        "accuracy_vs_fp64": res["fp64"],
-        "e2e": {"value": e2e_value, "unit": "DOF*steps/s", "h2d_bytes_per_step": res["h2d"],
-                "d2h_bytes_per_step": res["d2h"], "ms_per_step": res["e2e_ms"],
-                "first_call_with_build_ms": res["first_ms"]},
-        "gpu_launches": res["launches"] * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_axis0_r<256, VORTICITY, 2> (column pass)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": COLUMN_PASS_DRAM_BYTES,
-                     "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one stage-0 column pass "
-                                     "launch of this workload (bench.py --ncu-case)",
-                     "peak_source": f"{peak_kind} hbm_gbs",
-                     "per_kernel_ms": {k: v["avg_ms"] for k, v in res["prof"].items() if v["launches"]},
-                     "step_model_bytes_per_dof_step": 212,
-                     "step_achieved_gbs": 212.0 * dof_steps / world / (res["ms"] * 1e-3) / 1e9 * world},
-        "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")} if cpu else None,
-        "torch_gpu_reference": res["torch_ref"],
-        "reference_cpu": ref_cpu,
-        "clocks": res["clocks"],
-    }
-    tr = res["torch_ref"]
-    if tr and "value" in tr:
-        tr["fused_device_over_reference"] = value / tr["value"]
-        tr["fused_e2e_over_reference"] = e2e_value / tr["value"]
-    if ref_cpu and "value" in ref_cpu:
-        ref_cpu["fused_e2e_over_reference_cpu"] = e2e_value / ref_cpu["value"]
+    line = fused_line(res, args, world, cpu, ref_cpu)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -134,3 +134,36 @@ def test_reference_arm_prints_one_line_with_the_contract_keys():
     env.update(RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
     r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=600, cwd=repo)
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_fused_line_from_measurements():
+    import json
+    from types import SimpleNamespace
+
+    prof = {"column_pass": {"avg_ms": 0.06, "launches": 4000}, "row_pass": {"avg_ms": 0.024, "launches": 4000},
+            "prime": {"avg_ms": 0.05, "launches": 1}, "other": {"avg_ms": 0.0, "launches": 0}}
+    res = {"ms": 250.0, "e2e_ms": 251.0, "finite": True, "clocks": {"sm_mhz": 2070.0}, "launches": 64008,
+           "prof": prof, "h2d": 16777216, "d2h": 16777216, "B": 64,
+           "torch_ref": {"value": 1.7e9}, "fp64": {"rel_l2": 3e-7}, "first_ms": 400.0}
+    args = SimpleNamespace(steps=5, warmup=3)
+    cpu = {"value": 1.8e7, "unit": "DOF*steps/s", "cores": 16, "kind": "port", "sample": "s", "seconds": 1.0}
+    ref_cpu = {"value": 2.0e7}
+    line = bench.fused_line(res, args, 1, cpu, ref_cpu)
+    json.dumps(line)
+    dof_steps = 64 * 256 * 256 * 1000
+    assert math.isclose(line["value"], dof_steps / 0.25)
+    assert math.isclose(line["e2e"]["value"], dof_steps / 0.251)
+    assert line["e2e"]["first_call_with_build_ms"] == 400.0
+    assert line["config"]["rel_l2_vs_fp64"] == 3e-7 and line["accuracy_vs_fp64"] == {"rel_l2": 3e-7}
+    assert line["gpu_launches"] == 64008 * 5
+    assert math.isclose(line["roofline"]["achieved"], bench.column_pass_bytes(64) / 0.06e-3 / 1e9)
+    assert math.isclose(line["roofline"]["frac"], line["roofline"]["achieved"] / line["roofline"]["peak"])
+    assert set(line["roofline"]["per_kernel_ms"]) == {"column_pass", "row_pass", "prime"}
+    assert line["cpu_baseline"] == {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    assert math.isclose(line["torch_gpu_reference"]["fused_e2e_over_reference"], line["e2e"]["value"] / 1.7e9)
+    assert math.isclose(line["reference_cpu"]["fused_e2e_over_reference_cpu"], line["e2e"]["value"] / 2.0e7)
+    # N > 1: no CPU baselines, value is the whole job's
+    res2 = dict(res, torch_ref=None, fp64=None)
+    line2 = bench.fused_line(res2, args, 2, None, None)
+    assert line2["cpu_baseline"] is None and line2["reference_cpu"] is None
+    assert math.isclose(line2["value"], 2 * dof_steps / 0.25) and line2["config"]["rel_l2_vs_fp64"] is None

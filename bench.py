@@ -704,6 +704,19 @@ def run_burgers3d(args):
     dof_steps = 3 * n ** 3 * steps
     prof = profile_kernels(plan, state0, ws, device)
     finite = bool(torch.isfinite(torch.view_as_real(state)).all().item())
+    # e2e through the public API: pinned host field in, final field back to the host, every step
+    host_in = u0.cpu().pin_memory()
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out_h = op.integrate(u_0=host_in.to(device, non_blocking=True), dt=dt, step=steps).cpu()
+        if i >= args.warmup:
+            e2e_times.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = statistics.mean(e2e_times)
+    e2e = {"value": dof_steps / (e2e_ms * 1e-3), "unit": "DOF*steps/s", "h2d_bytes_per_step": host_in.numel() * 4,
+           "d2h_bytes_per_step": out_h.numel() * out_h.element_size(), "ms_per_step": e2e_ms}
+    del out_h
     R, why = _import_reference()
     if R is None:
         torch_ref = {"unavailable": why}
@@ -729,6 +742,7 @@ def run_burgers3d(args):
                        "l2": "inputs (200 MB state, 1.6 GB workspace) larger than L2",
                        "rel_l2_vs_fp64_after_50_steps": (fp64 or {}).get("rel_l2")},
             "accuracy_vs_fp64": fp64,
+            "e2e": e2e,
             "gpu_launches": plan.launch_count(steps, 1) * args.steps,
             "roofline": {"bound": "hbm", "per_kernel_ms": {k: v["avg_ms"] for k, v in prof.items() if v["launches"]},
                          "step_model_bytes_per_dof_step": 276,

@@ -97,3 +97,18 @@ def install(monkeypatch):
     monkeypatch.setattr(_native, "NativePlan", _CpuLinearPlan)
     monkeypatch.setattr(_native, "Spectral", _CpuSpectral)
     monkeypatch.setattr(_native, "_require_cuda", lambda t, what: None)
+
+
+def force_callback(monkeypatch):
+    """``install`` plus a lowering that refuses every nonlinear term, so that every nonlinear
+    program steps through the callback path (the fused programs included)."""
+    install(monkeypatch)
+    lower = _native.lower
+
+    def refuse_nonlinear(linear_terms, nonlinear_terms, *args, **kw):
+        if nonlinear_terms:
+            raise _lib.UnsupportedProgram(_lib.FSM_ERR_UNSUPPORTED, "forced onto the callback path")
+        return lower(linear_terms, nonlinear_terms, *args, **kw)
+
+    monkeypatch.setattr(_native, "lower", refuse_nonlinear)
+

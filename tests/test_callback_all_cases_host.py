@@ -19,7 +19,6 @@ import torch
 import cases as C
 import cpu_library as CL
 from oracle import spectral as S
-from torchfsm_gb300 import _lib, _native
 from torchfsm_gb300.integrator._callback import CallbackPlan
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -29,15 +28,7 @@ NAMES = sorted(n for n, c in C.CASES.items() if c.get("integrator") not in C.RK_
 
 @pytest.fixture
 def callback_everywhere(monkeypatch):
-    CL.install(monkeypatch)
-    lower = _native.lower
-
-    def refuse_nonlinear(linear_terms, nonlinear_terms, *args, **kw):
-        if nonlinear_terms:
-            raise _lib.UnsupportedProgram(_lib.FSM_ERR_UNSUPPORTED, "forced onto the callback path")
-        return lower(linear_terms, nonlinear_terms, *args, **kw)
-
-    monkeypatch.setattr(_native, "lower", refuse_nonlinear)
+    CL.force_callback(monkeypatch)
 
 
 @pytest.mark.parametrize("name", NAMES)

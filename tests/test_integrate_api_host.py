@@ -78,3 +78,19 @@ def test_contour_options_of_set_integrator():
     ref, _ = S.integrate(u0, mesh, [(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], [(-1.0, "convection")], 0.05,
                          40, n_integration_points=32, integration_radius=2.0)
     assert S.rel_l2(got, ref) <= TOL
+
+
+@pytest.mark.parametrize("fourier", [False, True])
+def test_empty_batch_returns_empty_results(fourier):
+    from torchfsm_gb300 import traj_recorder as TR
+
+    u0 = torch.zeros(0, 1, 64)
+    out = pde.Burgers(0.02).integrate(u_0=u0, mesh=MESH, dt=0.01, step=10, return_in_fourier=fourier)
+    assert out.shape == (0, 1, 64) and out.dtype == (torch.complex64 if fourier else torch.float32)
+    traj = pde.Burgers(0.02).integrate(u_0=u0.double(), mesh=MESH, dt=0.01, step=10,
+                                       trajectory_recorder=TR.AutoRecorder(TR.IntervalController(5)),
+                                       return_in_fourier=fourier)
+    assert traj.shape == (0, 3, 1, 64) and traj.dtype == (torch.complex128 if fourier else torch.float64)
+    u2 = torch.zeros(0, 2, 16, 16)
+    out2 = pde.Burgers(0.02).integrate(u_0=u2, mesh=[(0, 1, 16)] * 2, dt=0.01, step=3)
+    assert out2.shape == (0, 2, 16, 16)

@@ -22,7 +22,7 @@ from .. import _lib, _native
 from ..integrator import ETDRKIntegrator, RKIntegrator, SETDRKIntegrator
 from ..integrator._callback import CALLBACK_SCHEMES, CallbackPlan
 from ..mesh import FourierMesh, MeshGrid
-from ..traj_recorder import _TrajRecorder
+from ..traj_recorder import DiskRecorder, RandomBatchWisedRecorder, _TrajRecorder
 from ..utils import default
 
 MeshLike = Union[Sequence[Tuple[float, float, int]], MeshGrid, FourierMesh]
@@ -398,6 +398,8 @@ class OperatorLike(_MutableMixIn):
         value = u_0 if u_0 is not None else u_0_fft
         _native._require_cuda(value, "the initial condition")
         device = value.device
+        if value.shape[0] == 0:
+            return self._empty_integration(value, int(step), trajectory_recorder, return_in_fourier)
         integ = self._state_dict["integrator"]
         if integ is None or integ.dt != dt or integ.plan.device != device:
             self._build_integrator(dt, device)
@@ -457,6 +459,28 @@ class OperatorLike(_MutableMixIn):
         if return_in_fourier:
             return sp.half_to_full(state).to(cplx)
         return sp.to_physical(state, keep_input=False).to(real_dtype)
+
+    def _empty_integration(self, value: Tensor, step: int, recorder: Optional[_TrajRecorder],
+                           return_in_fourier: bool) -> Optional[Tensor]:
+        """The result of integrating an empty batch, with nothing launched: [0, C, n..] (or the
+        recorder's [0, T, C, n..]) in the dtype the call would return. The reference has no rule
+        for this case: its first forward transform raises on a batch of zero samples (MKL on the
+        CPU), so empty results are returned here instead of a library error."""
+        real_dtype = value.dtype if not value.is_complex() else value.real.dtype
+        cplx = torch.complex128 if real_dtype == torch.float64 else torch.complex64
+        dtype = cplx if return_in_fourier else real_dtype
+        lead = (0, self._state_dict["n_channel"])
+        shape = tuple(int(m[2]) for m in self._state_dict["f_mesh"].mesh_info)
+        if recorder is None:
+            return torch.empty(lead + shape, dtype=dtype, device=value.device)
+        recorder.return_in_fourier = return_in_fourier
+        if isinstance(recorder, DiskRecorder):
+            return None
+        if isinstance(recorder, RandomBatchWisedRecorder):
+            frames = recorder.n_recorded_frames
+        else:
+            frames = sum(1 for i in range(step + 1) if recorder.control_func(i))
+        return torch.empty((0, frames) + lead[1:] + shape, dtype=dtype, device=value.device)
 
     # -- one-shot evaluation -----------------------------------------------
     def _build_operator(self):

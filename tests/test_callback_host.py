@@ -100,3 +100,19 @@ def test_batched_linear_coefficient_matches_samples_run_alone(cpu_library):
         alone_op = float(nus[b]) * M.operator.Laplacian() + M.operator.ImplicitSource(C._allen_cahn_source)
         alone = alone_op.integrate(u_0=u0[b : b + 1], mesh=mesh, dt=0.01, step=40)
         assert S.rel_l2(both[b : b + 1].numpy(), alone.numpy()) <= 1e-6
+
+
+def test_per_sample_coefficient_on_a_nonlinear_term(cpu_library):
+    """A tensor coefficient [B, 1, 1] on the convection term (no fused kernel takes it) steps
+    through the callback path; each sample equals the FP64 oracle's run with its own scalar."""
+    M = C.namespace("torchfsm_gb300")
+    u0 = torch.tensor(C.initial_condition("allencahn1d_n64"), dtype=torch.float32)
+    mesh = [(0, 2 * np.pi, 64)]
+    coefs = torch.tensor([1.0, 0.5]).reshape(2, 1, 1)
+    op = 0.05 * M.operator.Laplacian() - coefs * M.operator.Convection()
+    both = op.integrate(u_0=u0, mesh=mesh, dt=0.01, step=30)
+    assert isinstance(op._state_dict["integrator"].plan, CallbackPlan)
+    for b in range(2):
+        ref, _ = S.integrate(u0[b : b + 1].double().numpy(), mesh, [(0.05, ("laplacian",))],
+                             [(-float(coefs[b]), "convection")], 0.01, 30)
+        assert S.rel_l2(both[b : b + 1].numpy(), ref) <= TOL

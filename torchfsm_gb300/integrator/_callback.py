@@ -107,6 +107,8 @@ class CallbackPlan:
                     u = sp.to_physical(half)
                     full = sp.half_to_full(half)
                 term = core(full, self.f_mesh, u)
+            if isinstance(coef, torch.Tensor):
+                coef = coef.to(term.device)  # a per-sample coefficient may live on the host
             term = coef * term
             result = term if result is None else result + term
         out = sp.full_to_half(result)

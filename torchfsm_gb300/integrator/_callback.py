@@ -80,8 +80,10 @@ class CallbackPlan:
             raise _lib.FsmError(_lib.FSM_ERR_INVALID, f"coefficient tables {tuple(tabs.shape)} for scheme {scheme}")
         lin_batch = max(1, int(getattr(linear_plan, "lin_batch", 1)))
         self.tables = tabs.reshape((ntab, lin_batch, entries // (S * lin_batch)) + self.half_shape)
-        keep = f_mesh.low_pass_filter(de_aliasing_rate)
-        self.keep_half = keep[..., :h].to(device=self.device, dtype=torch.float32)
+        self.keep_half = None
+        if f_mesh is not None:
+            keep = f_mesh.low_pass_filter(de_aliasing_rate)
+            self.keep_half = keep[..., :h].to(device=self.device, dtype=torch.float32)
 
     @property
     def handle(self):
@@ -167,3 +169,21 @@ class CallbackPlan:
         stages = {_lib.FSM_ETDRK1: 1, _lib.FSM_SETDRK1: 1, _lib.FSM_ETDRK2: 2, _lib.FSM_SETDRK2: 2,
                   _lib.FSM_SETDRK3: 3, _lib.FSM_SETDRK4: 4}[self.integrator]
         return int(steps) * stages * int(per_eval)
+
+
+class ClosurePlan(CallbackPlan):
+    """The callback path around one closure on full spectra: ``closure(u_hat)`` is the whole
+    nonlinear term (its dealiasing included), as an integrator constructed from the reference's
+    enum protocol receives it (``SETDRKIntegrator.SETDRK4.value(dt, linear_coef, nonlinear_func)``)."""
+
+    def __init__(self, linear_plan, closure: Callable[[torch.Tensor], torch.Tensor]):
+        super().__init__(linear_plan, [], None, 1.0)
+        self.closure = closure
+
+    def nonlinear(self, half: torch.Tensor) -> torch.Tensor:
+        sp = self.spectral
+        return sp.full_to_half(self.closure(sp.half_to_full(half))).to(torch.complex64)
+
+    def launch_count(self, steps: int, batch: int = 0) -> int:
+        return 0
+

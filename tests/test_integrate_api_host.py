@@ -94,3 +94,24 @@ def test_empty_batch_returns_empty_results(fourier):
     u2 = torch.zeros(0, 2, 16, 16)
     out2 = pde.Burgers(0.02).integrate(u_0=u2, mesh=[(0, 1, 16)] * 2, dt=0.01, step=3)
     assert out2.shape == (0, 2, 16, 16)
+
+
+def test_user_cores_through_the_plugin_points():
+    """A user LinearCoef (here nu * Laplacian written by hand) and a user NonlinearFunc (the
+    convection term written by hand) integrate like the built-in Burgers operator."""
+    from torchfsm_gb300.operator import LinearCoef, NonlinearFunc, Operator
+
+    class Diffusion(LinearCoef):
+        def __call__(self, f_mesh, n_channel):
+            return 0.02 * f_mesh.laplacian()
+
+    class Advection(NonlinearFunc):
+        def __call__(self, u_fft, f_mesh, u=None):
+            u = f_mesh.ifft(u_fft).real if u is None else u
+            return -f_mesh.fft(u * f_mesh.ifft(f_mesh.grad(0, 1) * u_fft).real)
+
+    u0 = _u0()
+    custom = Operator([lambda f_mesh, n: Diffusion(), lambda f_mesh, n: Advection()])
+    got = _run(custom, u0, mesh=MESH, dt=0.01, step=30)
+    ref, _ = S.integrate(u0, MESH, [(0.02, ("laplacian",))], [(-1.0, "convection")], 0.01, 30)
+    assert S.rel_l2(got, ref) <= TOL

@@ -91,3 +91,33 @@ def test_step_adjoint_rejects_null_arguments_without_gpu(libpath):
     assert lib.fsm_step_adjoint_workspace_bytes(None, 1, ctypes.byref(n)) == _lib.FSM_ERR_INVALID
     assert lib.fsm_step_adjoint(None, 1, None, None, None, None, None, 0, None) == _lib.FSM_ERR_INVALID
     assert "step_adjoint" in _lib.last_error()
+
+
+def test_descriptor_layouts_match_the_header(tmp_path):
+    """The ctypes descriptors the binding passes have the header's field offsets and sizes
+    (a C program compiled with the host compiler reports offsetof / sizeof)."""
+    import shutil
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"FsmMeshDesc": _lib.FsmMeshDesc, "FsmProgramDesc": _lib.FsmProgramDesc}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "torchfsm_gb300.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'  printf("{name} sizeof %zu\\n", sizeof({name}));')
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("{name} {field} %zu\\n", offsetof({name}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in filter(None, out):
+        struct, field, value = line.split()
+        got[(struct, field)] = int(value)
+    for name, cls in structs.items():
+        assert got[(name, "sizeof")] == ctypes.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert got[(name, field)] == getattr(cls, field).offset, (name, field)

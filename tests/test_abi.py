@@ -121,3 +121,21 @@ def test_descriptor_layouts_match_the_header(tmp_path):
         assert got[(name, "sizeof")] == ctypes.sizeof(cls), name
         for field, _ in cls._fields_:
             assert got[(name, field)] == getattr(cls, field).offset, (name, field)
+
+
+def test_binding_argument_counts_match_the_header(libpath):
+    """Every entry point the binding declares argtypes for takes as many arguments as its
+    prototype in the header."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    protos = dict(re.findall(r"\bint\s+(fsm_\w+)\s*\(([^)]*)\)", text))
+    lib = _lib.load(libpath)
+    checked = 0
+    for name, params in protos.items():
+        argtypes = getattr(lib, name).argtypes
+        if argtypes is None:
+            continue
+        params = params.strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(argtypes) == n, (name, len(argtypes), n)
+        checked += 1
+    assert checked >= len(protos) - 2  # the version and error queries may keep ctypes defaults

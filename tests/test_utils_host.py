@@ -68,3 +68,17 @@ def test_fused_programs_need_cuda_inputs():
     with pytest.raises(RuntimeError, match="CUDA"):
         pde.Burgers(0.01).integrate(u_0=torch.randn(1, 2, 16, 16), mesh=mesh, dt=0.01, step=2)
     assert fsm.Div()(u=torch.randn(1, 2, 16, 16), mesh=mesh).shape == (1, 1, 16, 16)
+
+
+def test_format_device_dtype():
+    import torch
+
+    # the reference's rules: no device -> CPU, "cuda" -> cuda:0, no dtype -> float32
+    assert U.format_device_dtype() == (torch.device("cpu"), torch.float32)
+    assert U.format_device_dtype("cuda") == (torch.device("cuda", 0), torch.float32)
+    assert U.format_device_dtype("cuda:1", torch.float64) == (torch.device("cuda", 1), torch.float64)
+    assert U.format_device_dtype("cpu")[0] == torch.device("cpu")
+    # a device object without an index is given index 0 as well, so that a mesh's device compares
+    # equal to its tensors' (the reference leaves such objects unchanged)
+    assert U.format_device_dtype(torch.device("cuda"))[0] == torch.device("cuda", 0)
+    assert U.default(None, 3) == 3 and U.default(0, 3) == 0

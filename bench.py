@@ -20,7 +20,9 @@ field, E(k) ~ k^4 exp(-(k/4)^2), zero mean, unit RMS).
              under baseline/_ref) on the same GPU, and on the host cores on a
              bounded sample of the batch.
   accuracy_vs_fp64 : the first samples of our result against the reference's
-             own integrator run in float64 on the GPU, all 1000 steps.
+             own integrator run in float64 on the GPU, after 10, 100 and 1000
+             steps, beside the reference's own float32 run of the same samples
+             against the same float64 run.
 
 Under torchrun every rank integrates its own batch of 64 (replicas, weak
 scaling, no collective on the data path); the time is the max over ranks.
@@ -55,6 +57,7 @@ MESH = [(0.0, 2 * math.pi, N), (0.0, 2 * math.pi, N)]
 METRIC = "DOF*steps/s (2D NS vorticity 256^2 x 64, SETDRK4, FP32)"
 WORKLOAD = "ns2d_vorticity_256x256_b64_1000steps"
 FP64_SAMPLES = 4  # samples of the batch integrated again by the reference in float64 (accuracy leg)
+ACCURACY_STEPS = (10, 100, 1000)  # step counts at which the accuracy leg compares the results
 
 
 def _peaks():
@@ -254,8 +257,12 @@ def run_fused(args, rank: int, world: int, dist) -> dict:
     fp64 = None
     if rank == 0 and not args.no_fp64_reference:
         w = w0 if w0.ndim == 4 else w0[:, None]
-        fp64 = fp64_reference_rel_l2(lambda R: R.pde.NavierStokesVorticity(RE), MESH, w[:FP64_SAMPLES], DT,
-                                     TIME_STEPS, out_h[:FP64_SAMPLES], device)
+        ours_by_step = {TIME_STEPS: out_h[:FP64_SAMPLES]}
+        for k in ACCURACY_STEPS:
+            if k != TIME_STEPS:
+                ours_by_step[k] = op.integrate(u_0=u_dev, dt=DT, step=k)[:FP64_SAMPLES].cpu()
+        fp64 = accuracy_by_step(lambda R: R.pde.NavierStokesVorticity(RE), MESH, w[:FP64_SAMPLES], DT,
+                                ACCURACY_STEPS, ours_by_step, device)
     return {"ms": ms, "e2e_ms": e2e_ms, "finite": finite, "clocks": clk.summary(), "launches": launches_per_step,
             "prof": prof, "h2d": host_in.numel() * 4, "d2h": out_h.numel() * out_h.element_size(),
             "B": B, "torch_ref": torch_ref, "fp64": fp64, "first_ms": first_ms}
@@ -422,6 +429,65 @@ def fp64_reference_rel_l2(make_op, mesh, u0: np.ndarray, dt: float, steps: int, 
         return {"rel_l2": err, "samples": int(u.shape[0]), "steps": steps, "reference_wall_s": wall,
                 "kind": f"reference integrate in float64 (complex128 transforms) on {ref.device.type}",
                 "version": getattr(R, "__version__", "0.0.4")}
+    except Exception as e:  # noqa: BLE001 -- the accuracy leg must not cost the throughput line
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def accuracy_by_step(make_op, mesh, u0: np.ndarray, dt: float, checkpoints, ours_by_step: dict, device) -> dict:
+    """Relative L2 distance from the reference's own float64 run at several step counts, for our
+    FP32 results and for the reference's own FP32 run of the same fields.
+
+    The unmodified reference (baseline/_ref) integrates ``u0`` twice with ``make_op(R).integrate``
+    on ``device`` and a recorder that keeps the frames at ``checkpoints``: once in float64 (complex128
+    transforms, FP64 contour coefficients: the reference follows the input's dtype,
+    ``operator/_base.py:553-559``) and once in float32. ``ours_by_step[k]`` is our result after k
+    steps from the same fields. Also reports, at the last checkpoint, the largest relative
+    difference of our energy spectrum from the FP64 one over the shells inside the 2/3 rule (the
+    comparison a chaotic run keeps). Failures are reported as ``unavailable``."""
+    import torch
+
+    R, why = _import_reference()
+    if R is None:
+        return {"unavailable": why}
+    try:
+        ks = sorted(int(k) for k in checkpoints)
+        wanted = set(ks)
+
+        def run(dtype):
+            rec = R.traj_recorder.AutoRecorder(control_func=lambda s: s in wanted)
+            u = torch.tensor(np.asarray(u0), dtype=dtype, device=device)
+            t0 = time.perf_counter()
+            traj = make_op(R).integrate(u_0=u, mesh=mesh, dt=dt, step=ks[-1], trajectory_recorder=rec)
+            if traj.device.type == "cuda":
+                torch.cuda.synchronize(traj.device)
+            return traj, time.perf_counter() - t0
+
+        ref64, wall = run(torch.float64)
+        ref32, _ = run(torch.float32)
+        if ref64.dtype != torch.float64 or ref64.shape[1] != len(ks):
+            return {"unavailable": f"reference trajectory {ref64.dtype} {tuple(ref64.shape)}"}
+
+        def rel(a, b):
+            return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+        ours, theirs = {}, {}
+        for i, k in enumerate(ks):
+            r = ref64[:, i]
+            theirs[str(k)] = rel(ref32[:, i].to(torch.float64), r)
+            if k in ours_by_step:
+                o = torch.as_tensor(ours_by_step[k]).to(device=r.device, dtype=torch.float64).reshape(r.shape)
+                ours[str(k)] = rel(o, r)
+        res = {"rel_l2": ours.get(str(ks[-1])), "by_step": ours, "reference_fp32_by_step": theirs,
+               "samples": int(ref64.shape[0]), "steps": ks[-1], "reference_wall_s": wall,
+               "kind": f"reference integrate in float64 (complex128 transforms) on {ref64.device.type}",
+               "version": getattr(R, "__version__", "0.0.4")}
+        if ks[-1] in ours_by_step:
+            o = torch.as_tensor(ours_by_step[ks[-1]]).to(dtype=torch.float64).reshape(ref64[:, -1].shape)
+            e_ours, e_ref = energy_spectrum(o), energy_spectrum(ref64[:, -1])
+            kmax = int(2.0 / 3.0 * (min(o.shape[2:]) // 2))
+            sel = e_ref[1:kmax + 1]
+            res["energy_spectrum_max_rel_diff"] = float(((e_ours[1:kmax + 1] - sel).abs() / sel).max())
+        return res
     except Exception as e:  # noqa: BLE001 -- the accuracy leg must not cost the throughput line
         return {"unavailable": f"{type(e).__name__}: {e}"}
 

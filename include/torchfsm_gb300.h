@@ -137,8 +137,11 @@ int fsm_plan_set_batch_dt(FsmPlan* plan, int32_t b, double dt, void* stream);
 int fsm_plan_move_batch(FsmPlan* plan, int32_t dst, int32_t src, void* stream);
 
 /* Copy the plan's coefficient tables (complex64, [ntab][table_batch][lin_channel][S], the
- * scheme's order: SETDRK4 E, E2, c1, c4, c5, c6) to the device buffer dst of
- * capacity_bytes; with dst == NULL only report ntab and the entries per table.
+ * scheme's order: SETDRK4 E - 1, E2 - 1, c1, c4, c5, c6) to the device buffer dst of
+ * capacity_bytes; with dst == NULL only report ntab and the entries per table. The exponential
+ * tables (E = exp(dt L), E2 = exp(dt L / 2); table 0 of every ETD scheme, table 1 of SETDRK3/4)
+ * hold E - 1: the kernels form E u as u + (E - 1) u, which keeps E's FP32 rounding error from
+ * compounding over the steps.
  * Inspection of UnCachedSETDRK*.__init__'s tables (integrator/_stable_etdrk/_uncached.py:180-211). */
 int fsm_plan_tables(const FsmPlan* plan, void* dst, size_t capacity_bytes, int32_t* ntab, int64_t* entries,
                     void* stream);

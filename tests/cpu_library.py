@@ -4,9 +4,9 @@
 
 * ``_native.NativePlan`` by a plan of a linear part whose coefficient tables are the oracle's
   FP64 tables of the same linear symbol, laid out as the library lays them out
-  (``fsm_plan_tables``: [tables][lin_batch][lin_channel][half spectrum], per scheme E, E2,
-  c1.. in the library's order), and which steps linear ETDRK0 programs as the pointwise
-  kernel does (every point times E per step);
+  (``fsm_plan_tables``: [tables][lin_batch][lin_channel][half spectrum], per scheme E - 1,
+  E2 - 1, c1.. in the library's order), and which steps linear ETDRK0 programs as the pointwise
+  kernel does (every point plus (E - 1) times itself per step);
 * ``_native.Spectral``'s forward and inverse transforms by torch's real FFTs;
 * the CUDA-input check by a no-op,
 
@@ -35,7 +35,9 @@ def _library_tables(integrator: int, lin: np.ndarray, dt: float, m: int, r: floa
         t = S.setdrk_coefs(order, lin, dt, m, r)
         keys = {1: ["E", "c1"], 2: ["E", "c1", "c2"], 3: ["E", "E2", "c1", "c2", "c3", "c4", "c5"],
                 4: ["E", "E2", "c1", "c4", "c5", "c6"]}[order]
-    return [np.broadcast_to(np.asarray(t[k], dtype=np.complex128), lin.shape) for k in keys]
+    # the exponential tables are stored as E - 1 (the library's layout)
+    return [np.broadcast_to(np.asarray(t[k], dtype=np.complex128) - (1.0 if k in ("E", "E2") else 0.0), lin.shape)
+            for k in keys]
 
 
 class _CpuLinearPlan:
@@ -72,11 +74,11 @@ class _CpuLinearPlan:
         """Linear programs (ETDRK0): every point advances by E per step, as the pointwise kernel."""
         if self.integrator != _lib.FSM_ETDRK0:
             raise NotImplementedError("the CPU stand-in steps linear ETDRK0 programs only")
-        E = self.tables()[0].reshape(self._lin_shape)
+        Em1 = self.tables()[0].reshape(self._lin_shape)
         for i in range(steps):
             if slots is not None and slots[i] >= 0:
                 traj[:, slots[i]] = state
-            state.mul_(E)
+            state.add_(Em1 * state)
         if slots is not None and slots[steps] >= 0:
             traj[:, slots[steps]] = state
 

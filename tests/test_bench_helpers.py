@@ -45,6 +45,34 @@ def test_fp64_accuracy_leg_runs_the_reference_in_float64():
     assert 1e-9 < r32["rel_l2"] < 1e-5, r32
 
 
+def test_accuracy_by_step_compares_ours_and_the_reference_fp32_with_fp64():
+    """The per-step accuracy leg: the oracle's FP64 results stand in for ours and land at FP64
+    round-off of the reference's float64 run at every checkpoint; the reference's own float32 run
+    lands inside the 1e-5 bar but above round-off; the energy-spectrum figure is reported."""
+    import numpy as np
+    import pytest
+
+    R, why = bench._import_reference()
+    if R is None:
+        pytest.skip(why)
+    from oracle import spectral as S
+    from torchfsm_gb300 import initial
+
+    mesh = [(0.0, 2 * math.pi, 32)] * 2
+    w0 = initial.gaussian_random_field((32, 32), 2, 1, initial.vorticity_spectrum, 5)
+    w0 = w0 if w0.ndim == 4 else w0[:, None]
+    dt = 1e-3
+    ours = {}
+    for k in (4, 12):
+        ours[k], _ = S.integrate(w0, mesh, [(1e-3, ("laplacian",))], [(-1.0, "vorticity_convection")], dt, k)
+    r = bench.accuracy_by_step(lambda R: R.pde.NavierStokesVorticity(1000.0), mesh, w0, dt, (4, 12), ours, "cpu")
+    assert set(r["by_step"]) == {"4", "12"} and set(r["reference_fp32_by_step"]) == {"4", "12"}, r
+    assert max(r["by_step"].values()) < 1e-10, r
+    assert r["rel_l2"] == r["by_step"]["12"]
+    assert all(1e-9 < v < 1e-5 for v in r["reference_fp32_by_step"].values()), r
+    assert r["energy_spectrum_max_rel_diff"] < 1e-8, r
+
+
 def test_fp64_accuracy_leg_reports_failure_instead_of_raising():
     import numpy as np
     import pytest

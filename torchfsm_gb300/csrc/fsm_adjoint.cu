@@ -116,7 +116,7 @@ __device__ __forceinline__ float adj_point(const AdjGeom& g, int64_t s, float (&
   return m;
 }
 
-// Real parts of the plan's coefficient tables (SETDRK4 order E, E2, c1, c4, c5, c6).
+// Real parts of the plan's coefficient tables (SETDRK4 order E - 1, E2 - 1, c1, c4, c5, c6).
 struct AdjTabs {
   const float2* tab;
   int64_t ts;
@@ -131,6 +131,8 @@ __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y
 __device__ __forceinline__ float2 sc(float2 a, float k) { return make_float2(k * a.x, k * a.y); }
 __device__ __forceinline__ float2 ad(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float redot(float2 a, float2 b) { return a.x * b.x + a.y * b.y; }  // Re(conj(a) b)
+// E a from the table value em1 = E - 1 (real): a + em1 a
+__device__ __forceinline__ float2 xe(float2 a, float em1) { return make_float2(fmaf(em1, a.x, a.x), fmaf(em1, a.y, a.y)); }
 
 // Stage input a = x (combine 0) or E2 x + c1 (alpha y + beta z) (z may be null), optionally stored,
 // and the fields of the nonlinear term: F[0] = m a, F[1 + i] = i k_i m a ([1 + nd][B][C][S]).
@@ -146,7 +148,7 @@ __global__ void k_adjs_fields(AdjGeom g, AdjTabs T, int64_t total, int C, int co
     if (combine) {
       float2 r = sc(y[q], alpha);
       if (z) r = ad(r, sc(z[q], beta));
-      a = ad(sc(a, T(1, b, c, s)), sc(r, T(2, b, c, s)));
+      a = ad(xe(a, T(1, b, c, s)), sc(r, T(2, b, c, s)));
       if (store) store[q] = a;
     }
     float k[3];
@@ -183,7 +185,7 @@ __global__ void k_adjs_begin(AdjTabs T, int64_t total, int C, const float2* __re
     const int c = (int)((q / S) % C);
     const int64_t b = q / ((int64_t)C * S);
     const float2 v = ub[q];
-    ubar[q] = sc(v, T(0, b, c, s));
+    ubar[q] = xe(v, T(0, b, c, s));
     n0b[q] = sc(v, T(3, b, c, s));
     const float2 w = sc(v, 2.f * T(4, b, c, s));
     n1b[q] = w;
@@ -227,9 +229,9 @@ __global__ void k_adjs_end(AdjGeom g, AdjTabs T, int64_t total, int C, float inv
       e.out[q] = ad(e.ubar[q], abar);
       continue;
     }
-    const float E2 = T(1, b, c, s), c1 = T(2, b, c, s);
+    const float E2m1 = T(1, b, c, s), c1 = T(2, b, c, s);
     if (mode == 3) {
-      e.a1b[q] = sc(abar, E2);
+      e.a1b[q] = xe(abar, E2m1);
       e.nbs[q] = ad(e.n2b[q], sc(abar, 2.f * c1));
       const float2 n0 = e.n0[q];
       e.n0b[q] = ad(e.n0b[q], sc(abar, -c1));
@@ -238,7 +240,7 @@ __global__ void k_adjs_end(AdjGeom g, AdjTabs T, int64_t total, int C, float inv
         e.tb[2 * total + q] += (double)redot(abar, ad(sc(e.n2[q], 2.f), sc(n0, -1.f)));
       }
     } else if (mode == 2) {
-      e.ubar[q] = ad(e.ubar[q], sc(abar, E2));
+      e.ubar[q] = ad(e.ubar[q], xe(abar, E2m1));
       e.nbs[q] = ad(e.n1b[q], sc(abar, c1));
       if (e.tb) {
         e.tb[total + q] += (double)redot(abar, e.u[q]);
@@ -246,7 +248,7 @@ __global__ void k_adjs_end(AdjGeom g, AdjTabs T, int64_t total, int C, float inv
       }
     } else {
       const float2 t = ad(e.a1b[q], abar);
-      e.ubar[q] = ad(e.ubar[q], sc(t, E2));
+      e.ubar[q] = ad(e.ubar[q], xe(t, E2m1));
       e.nbs[q] = ad(e.n0b[q], sc(t, c1));
       if (e.tb) {
         e.tb[total + q] += (double)redot(t, e.u[q]);

@@ -71,9 +71,19 @@ __device__ __forceinline__ cd cexpd(cd z) {
   return mk(e * c, e * s);
 }
 __device__ __forceinline__ float2 tof(cd z) { return make_float2((float)z.x, (float)z.y); }
+// exp(z) - 1 without the cancellation of exp(z) - 1 near z = 0:
+// Re = e^x cos y - 1 = expm1(x) cos y - 2 sin^2(y/2), Im = e^x sin y.
+__device__ __forceinline__ cd cexpm1d(cd z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double em = expm1(z.x);
+  const double sh = sin(0.5 * z.y);
+  return mk(em * c - 2.0 * sh * sh, (em + 1.0) * s);
+}
 
 // One thread per (batch, channel, point) entry of L. Tables (float2) are
-// written at tab[t * ts + idx] in the scheme's order (fsm_common.cuh).
+// written at tab[t * ts + idx] in the scheme's order (fsm_common.cuh); the exponential tables
+// hold exp(dt L) - 1 and exp(dt L / 2) - 1.
 // SETDRK: phi-functions as the mean over M contour points z_j = r e^{i pi (2j-1)/M} + dt L
 // of the Kassam-Trefethen integrands, real part kept (integrator/_stable_etdrk/_uncached.py:8-43, 46-211);
 // ETDRK1/2: closed forms with the L == 0 limits (integrator/_etdrk.py:30-82).
@@ -96,15 +106,15 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
     tab[ts + idx] = make_float2((float)dt, 0.f);
     return;
   }
-  const cd E = cexpd(hl);
-  tab[idx] = tof(E);
+  const cd Em1 = cexpm1d(hl);
+  tab[idx] = tof(Em1);
   if (integ == FSM_ETDRK0) return;
   if (integ == FSM_ETDRK1 || integ == FSM_ETDRK2) {
     const bool zero = (l.x == 0.0 && l.y == 0.0);
-    const cd c1 = zero ? mk(dt, 0.0) : cdiv(E - mk(1.0, 0.0), l);
+    const cd c1 = zero ? mk(dt, 0.0) : cdiv(Em1, l);
     tab[ts + idx] = tof(c1);
     if (integ == FSM_ETDRK2) {
-      const cd c2 = zero ? mk(0.5 * dt, 0.0) : cdiv(E - mk(1.0, 0.0) - hl, dt * (l * l));
+      const cd c2 = zero ? mk(0.5 * dt, 0.0) : cdiv(Em1 - hl, dt * (l * l));
       tab[2 * ts + idx] = tof(c2);
     }
     return;
@@ -171,7 +181,7 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
       tab[2 * ts + idx] = re(s_e2);
       break;
     case FSM_SETDRK3:
-      tab[ts + idx] = tof(cexpd(0.5 * hl));
+      tab[ts + idx] = tof(cexpm1d(0.5 * hl));
       tab[2 * ts + idx] = re(s_h);
       tab[3 * ts + idx] = re(s_e1);
       tab[4 * ts + idx] = re(s_a);
@@ -180,7 +190,7 @@ __global__ void k_phi_tables(const double2* __restrict__ L, int64_t lcount, int6
       break;
     case FSM_SETDRK4:
     default:
-      tab[ts + idx] = tof(cexpd(0.5 * hl));
+      tab[ts + idx] = tof(cexpm1d(0.5 * hl));
       tab[2 * ts + idx] = re(s_h);
       tab[3 * ts + idx] = re(s_a);
       tab[4 * ts + idx] = re(s_b);
@@ -208,7 +218,7 @@ __global__ void k_pointwise(StepArgs a, int64_t total) {
     if (slot0 >= 0) a.traj[(((int64_t)b * a.n_frames + slot0) * C + c) * S + s] = u;
     for (int step = 0; step < a.steps; ++step) {
       if (a.integ == FSM_ETDRK0) {
-        u = cmul(tab[0], u);
+        u = cexpmul(tab[0], u);
       } else {
         for (int st = 0; st < a.nstages; ++st) (void)etd_stage(a.integ, st, nv, &u, aux, aux + 1, tab, a.ts, 1);
       }

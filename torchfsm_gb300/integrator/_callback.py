@@ -118,29 +118,37 @@ class CallbackPlan:
 
     # -- one step ---------------------------------------------------------------
     def step(self, u: torch.Tensor) -> torch.Tensor:
-        """One step of the scheme on the half spectra ``u`` [B, C, ...] (complex64)."""
+        """One step of the scheme on the half spectra ``u`` [B, C, ...] (complex64).
+
+        The library's exponential tables hold exp(dt L) - 1 (and exp(dt L / 2) - 1), so
+        exp(dt L) u is formed as u + (E - 1) u, as the kernels form it."""
         T, N, s = self.tables, self.nonlinear, self.integrator
+
+        def ex(em1, v):
+            return v + em1 * v
+
         if s in (_lib.FSM_ETDRK1, _lib.FSM_SETDRK1):
-            return T[0] * u + T[1] * N(u)
+            return ex(T[0], u) + T[1] * N(u)
         if s in (_lib.FSM_ETDRK2, _lib.FSM_SETDRK2):
             n0 = N(u)
-            a1 = T[0] * u + T[1] * n0
+            a1 = ex(T[0], u) + T[1] * n0
             return a1 + T[2] * (N(a1) - n0)
         if s == _lib.FSM_SETDRK3:
             n0 = N(u)
-            a1 = T[1] * u + T[2] * n0
+            a1 = ex(T[1], u) + T[2] * n0
             n1 = N(a1)
-            a2 = T[0] * u + T[3] * (2 * n1 - n0)
+            Eu = ex(T[0], u)
+            a2 = Eu + T[3] * (2 * n1 - n0)
             n2 = N(a2)
-            return T[0] * u + T[4] * n0 + T[5] * n1 + T[6] * n2
+            return Eu + T[4] * n0 + T[5] * n1 + T[6] * n2
         n0 = N(u)  # SETDRK4
-        a1 = T[1] * u + T[2] * n0
+        a1 = ex(T[1], u) + T[2] * n0
         n1 = N(a1)
-        a2 = T[1] * u + T[2] * n1
+        a2 = ex(T[1], u) + T[2] * n1
         n2 = N(a2)
-        a3 = T[1] * a1 + T[2] * (2 * n2 - n0)
+        a3 = ex(T[1], a1) + T[2] * (2 * n2 - n0)
         n3 = N(a3)
-        return T[0] * u + T[3] * n0 + T[4] * 2 * (n1 + n2) + T[5] * n3
+        return ex(T[0], u) + T[3] * n0 + T[4] * 2 * (n1 + n2) + T[5] * n3
 
     @torch.no_grad()
     def integrate_half(self, state: torch.Tensor, steps: int, slots: Optional[Sequence[int]] = None,

@@ -245,6 +245,64 @@ CASES.update({
 })
 
 
+# Cases at the benchmarked kernel instances (the 256-point register transforms of the 2D plane
+# passes and of each 3D axis, the split launch of a large 2D batch, and the 1D line kernel at the
+# serving sizes). Their batches are too large to store: the fixture keeps the samples named in
+# ``keep`` (final physical fields, float32) and every sample's L2 norm (float64), the GPU test
+# runs the whole batch, and the oracle test integrates the ``oracle_samples`` alone (every sample
+# of these programs evolves independently).
+LARGE_CASES = {
+    # 2D vorticity NS at the headline's grid, dt and viscosity, the first 48 of its seeded fields: a
+    # batch of 48 x 256 x 129 spectral points runs split into parts on forked streams.
+    "ns2d_n256_b48": dict(
+        mesh=[(0, TWO_PI, 256), (0, TWO_PI, 256)], batch=48, channels=1, dt=1e-3, step=50, record=0,
+        build=lambda M: M.pde.NavierStokesVorticity(1000),
+        lin=[(1.0 / 1000, ("laplacian",))], nl=[(-1.0, "vorticity_convection")],
+        ic=_grf2(2024, 256), keep=[0, 13, 31, 47], oracle_samples=[0],
+    ),
+    # 2D Burgers at the serving stream's largest grid (two velocity channels).
+    "burgers2d_n256": dict(
+        mesh=[(0, TWO_PI, 256), (0, TWO_PI, 256)], batch=2, channels=2, dt=0.01, step=30, record=0,
+        build=lambda M: M.pde.Burgers(0.01),
+        lin=[(0.01, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(251, (256, 256), 8, 0.25), keep=[1], oracle_samples=[1],
+    ),
+    # 3D Burgers with one axis of 256 points each: the x pass, the y passes and the z pass of the
+    # 256^3 workload at their 256-point instances.
+    "burgers3d_256x16x16": dict(
+        mesh=[(0, TWO_PI, 256), (0, TWO_PI, 16), (0, TWO_PI, 16)], batch=1, channels=3, dt=5e-3, step=20, record=0,
+        build=lambda M: M.pde.Burgers(0.005),
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(261, (256, 16, 16), 3, 1.0), keep=[0], oracle_samples=[0],
+    ),
+    "burgers3d_16x256x16": dict(
+        mesh=[(0, TWO_PI, 16), (0, TWO_PI, 256), (0, TWO_PI, 16)], batch=1, channels=3, dt=5e-3, step=20, record=0,
+        build=lambda M: M.pde.Burgers(0.005),
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(262, (16, 256, 16), 3, 1.0), keep=[0], oracle_samples=[0],
+    ),
+    "burgers3d_16x16x256": dict(
+        mesh=[(0, TWO_PI, 16), (0, TWO_PI, 16), (0, TWO_PI, 256)], batch=1, channels=3, dt=5e-3, step=20, record=0,
+        build=lambda M: M.pde.Burgers(0.005),
+        lin=[(0.005, ("laplacian",))], nl=[(-1.0, "convection")],
+        ic=_bl(263, (16, 16, 256), 3, 1.0), keep=[0], oracle_samples=[0],
+    ),
+    # 1D Kuramoto-Sivashinsky on L = 32 pi at two of the serving stream's sizes.
+    "ks1d_n1024": dict(
+        mesh=[(0, 32 * math.pi, 1024)], batch=3, channels=1, dt=0.05, step=200, record=0,
+        build=lambda M: M.pde.KuramotoSivashinsky(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "convection")],
+        ic=_bl(271, (1024,), 8, 1.0), keep=[0, 1, 2], oracle_samples=[0, 1, 2],
+    ),
+    "ks1d_n4096": dict(
+        mesh=[(0, 32 * math.pi, 4096)], batch=3, channels=1, dt=0.02, step=200, record=0,
+        build=lambda M: M.pde.KuramotoSivashinsky(),
+        lin=[(-1.0, ("laplacian",)), (-1.0, ("biharmonic",))], nl=[(-1.0, "convection")],
+        ic=_bl(272, (4096,), 8, 1.0), keep=[0, 1, 2], oracle_samples=[0, 1, 2],
+    ),
+}
+
+
 def _allen_cahn_source(u):
     return u - u ** 3
 
@@ -298,7 +356,10 @@ CALLBACK_CASES = {
 
 
 def _case(name: str) -> dict:
-    return CASES[name] if name in CASES else CALLBACK_CASES[name]
+    for table in (CASES, LARGE_CASES, CALLBACK_CASES):
+        if name in table:
+            return table[name]
+    raise KeyError(name)
 
 
 def set_case_integrator(op, M, kind):
@@ -325,7 +386,7 @@ def record_fn(name: str):
 
 def oracle_terms(name: str):
     """Linear and nonlinear term lists in the oracle's vocabulary (sources resolved to spectra)."""
-    c = CASES[name]
+    c = _case(name)
     nl = []
     for coef, spec in c["nl"]:
         if isinstance(spec, tuple) and spec[0] == "source_phys":

@@ -1,7 +1,7 @@
 """Generate tests/golden/algebra_reference.npz: operator expressions built with the reference's
 algebra (torchfsm/operator/_base.py:170-206, 826-1028) and evaluated once, in float64 on the CPU.
 
-    python tests/golden/make_algebra_golden.py /root/reference
+    python tests/golden/make_algebra_golden.py <reference source tree>
 
 ``EXPRESSIONS`` lists each expression as a name, a mesh, the input field's channels and a function
 of a torchfsm-like namespace returning the operator; the file holds the reference's result of
@@ -89,4 +89,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

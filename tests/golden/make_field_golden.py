@@ -1,7 +1,7 @@
 """Generate tests/golden/field_helpers.npz by running the reference's initial-condition helpers
 (torchfsm/field.py) under fixed torch seeds.
 
-    python tests/golden/make_field_golden.py /root/reference
+    python tests/golden/make_field_golden.py <reference source tree>
 
 ``CALLS`` lists each helper call: a name, the torch seed set before it, and a function that
 makes the call on a given ``field`` module (the reference's when generating, torchfsm_gb300's in
@@ -66,4 +66,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

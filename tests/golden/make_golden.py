@@ -2,7 +2,7 @@
 
 Run in a container where the reference (torchfsm 0.0.4) is importable:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference source tree>
 
 The reference is imported from the given source tree and run on the CPU in
 float64 for every case of ``cases.py`` (``CASES`` and ``CALLBACK_CASES``); the
@@ -72,6 +72,23 @@ def main(ref_root: str) -> None:
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **payload)
         print(name, payload["final"].shape, payload["integrator"])
 
+    # Large batches at the benchmarked kernel instances: the kept samples' final fields and every
+    # sample's L2 norm.
+    for name, case in C.LARGE_CASES.items():
+        if only and name not in only:
+            continue
+        u0 = C.initial_condition(name)
+        op = case["build"](M)
+        out = op.integrate(u_0=torch.tensor(u0, dtype=torch.float64), mesh=case["mesh"], dt=case["dt"],
+                           step=case["step"]).numpy()
+        keep = np.asarray(case["keep"], dtype=np.int64)
+        kept = out[keep]
+        norms = np.sqrt((out.reshape(out.shape[0], -1) ** 2).sum(axis=1))
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), keep=keep,
+                            final_kept=kept if kept.size <= 131072 else kept.astype(np.float32), norms=norms,
+                            integrator=np.array(type(op._state_dict["integrator"]).__name__))
+        print(name, kept.shape, "norms", norms.min(), norms.max())
+
     # One-shot evaluation (Operator.__call__, solve, functional.*) in float64.
     for name, case in C.APPLY_CASES.items():
         if only and name not in only:
@@ -140,4 +157,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

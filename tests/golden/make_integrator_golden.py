@@ -3,7 +3,7 @@
 ``ETDRKIntegrator.ETDRK0.value(dt, linear_coef)``, ``RKIntegrator.RK4.value()``; operator/_base.py
 :441-526) and stepped by hand, in float64 on the CPU.
 
-    python tests/golden/make_integrator_golden.py /root/reference
+    python tests/golden/make_integrator_golden.py <reference source tree>
 
 ``problem()`` builds the linear coefficient, the nonlinear function (a dealiased Burgers-type term
 written with torch only, so both packages get the same callable) and the initial spectrum;
@@ -89,4 +89,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

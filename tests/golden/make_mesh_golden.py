@@ -1,7 +1,7 @@
 """Generate tests/golden/mesh_reference.npz by querying the reference's mesh classes
 (torchfsm/mesh.py: MeshGrid, FFTFrequency, BroadcastedFFTFrequency, FourierMesh, mesh_shape).
 
-    python tests/golden/make_mesh_golden.py /root/reference
+    python tests/golden/make_mesh_golden.py <reference source tree>
 
 ``QUERIES`` lists each query: a name and a function of the mesh module that returns a tensor or
 a tuple of ints; ``tests/test_mesh_host.py`` runs the same queries on torchfsm_gb300.mesh. The
@@ -71,4 +71,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

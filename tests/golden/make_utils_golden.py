@@ -1,7 +1,7 @@
 """Generate tests/golden/utils_helpers.npz by running the reference's trajectory helpers
 (torchfsm/utils.py:44-183) on a small seeded trajectory.
 
-    python tests/golden/make_utils_golden.py /root/reference
+    python tests/golden/make_utils_golden.py <reference source tree>
 
 For each helper and torch seed the file holds the reference's output; the statistics are
 stored per channel. The reference is imported from the given source tree (CPU only).
@@ -44,4 +44,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("TORCHFSM_REFERENCE")
+    if not ref:
+        sys.exit(f"usage: python {os.path.relpath(__file__)} <reference source tree> (or set TORCHFSM_REFERENCE)")
+    main(ref)

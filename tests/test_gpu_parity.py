@@ -47,6 +47,24 @@ def test_matches_reference_fp64(name):
     assert err <= TOL, f"{name}: rel-L2 {err:.3e} > {TOL}"
 
 
+@pytest.mark.parametrize("name", sorted(C.LARGE_CASES))
+def test_benchmarked_instances_match_reference_fp64(name):
+    """The whole batch through the public API; the fixture's kept samples against the reference's
+    FP64 fields and every sample's L2 norm against the reference's (the whole batch at once: a
+    wrongly handled part of a split launch shows in its samples' norms)."""
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    out = _run(name).cpu().numpy().astype(np.float64)
+    keep = g["keep"]
+    ref = g["final_kept"].astype(np.float64)
+    assert out.shape[0] == g["norms"].shape[0] and out[keep].shape == ref.shape
+    err = max(S.rel_l2(out[k], ref[i]) for i, k in enumerate(keep))
+    norms = np.sqrt((out.reshape(out.shape[0], -1) ** 2).sum(axis=1))
+    norm_err = float(np.max(np.abs(norms - g["norms"]) / g["norms"]))
+    print(f"{name}: rel-L2 {err:.3e} (kept samples), worst relative norm error {norm_err:.3e}")
+    assert err <= TOL, f"{name}: rel-L2 {err:.3e} > {TOL}"
+    assert norm_err <= TOL, f"{name}: norm error {norm_err:.3e} > {TOL}"
+
+
 def test_deterministic():
     a = _run("ns2d_n32")
     b = _run("ns2d_n32")

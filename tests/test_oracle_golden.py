@@ -37,6 +37,23 @@ def test_oracle_matches_reference(name):
         assert S.rel_l2(traj, g["traj"]) < tol(g["traj"])
 
 
+@pytest.mark.parametrize("name", sorted(C.LARGE_CASES))
+def test_oracle_matches_reference_large(name):
+    """The oracle on the samples of a large case that it integrates alone, against the reference's
+    fields of the same samples (stored in float32 above 131072 values)."""
+    case = C.LARGE_CASES[name]
+    g = _load(name)
+    keep = list(g["keep"])
+    u0 = C.initial_condition(name)
+    lin, nl = C.oracle_terms(name)
+    for b in case["oracle_samples"]:
+        final, _ = S.integrate(u0[b:b + 1], case["mesh"], lin, nl, case["dt"], case["step"])
+        ref = g["final_kept"][keep.index(b)]
+        tol = 1e-10 if ref.dtype == np.float64 else 1e-6
+        assert S.rel_l2(final[0], ref) < tol
+        assert abs(np.sqrt((final ** 2).sum()) - g["norms"][b]) < tol * g["norms"][b]
+
+
 @pytest.mark.parametrize("tag,dt_mesh", [
     ("ks1d", [(0, 32 * np.pi, 64)]),
     ("ns2d", [(0, 2 * np.pi, 32)] * 2),

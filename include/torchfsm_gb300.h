@@ -185,8 +185,13 @@ int fsm_integrate_profiled(const FsmPlan* plan, int32_t batch, void* state, int3
  * whose scratch would exceed the array (fsm_plan_workspace_bytes) is rejected
  * with FSM_ERR_INVALID. It runs one launch sequence on `stream` (never the
  * library's own streams of a split batch). The first call on a device looks up
- * the array's device address and must come before any stream capture on that device. All calls
- * share the one array: calls that overlap on the GPU (other streams, other
+ * the array's device address and must come before any stream capture on that device. With
+ * CUDA's lazy module loading (the default), that first call, and the first launch of each
+ * kernel a plan uses, load code and back the array, which can allocate: make one warm-up call
+ * per device and plan at start-up, before the region that may not allocate; later calls
+ * allocate nothing. The address is cached per device index for the life of the process:
+ * cudaDeviceReset (or any reset of the primary context) is not supported after the first
+ * call. All calls share the one array: calls that overlap on the GPU (other streams, other
  * threads) race and corrupt each other's results; serialise them. No
  * counterpart in the reference. */
 int fsm_integrate_static(const FsmPlan* plan, int32_t batch, void* state, int32_t steps, void* stream);

@@ -64,6 +64,25 @@ def test_static_entry_matches_workspace_entry_on_two_calls():
         assert bool(torch.isfinite(torch.view_as_real(got)).all())
 
 
+def test_static_entry_allocates_nothing_after_a_warm_up_call():
+    """The promise the entry point exists for: after one warm-up call (which loads the kernels
+    and backs the array), further calls leave the device's free memory unchanged."""
+    lib = _lib.load()
+    op, plan, state0 = _plan_and_state()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    got = state0.clone()
+    rc = lib.fsm_integrate_static(plan.handle, BATCH, ctypes.c_void_p(got.data_ptr()), STEPS, stream)
+    assert rc == _lib.FSM_OK, _lib.last_error()
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    for _ in range(2):
+        rc = lib.fsm_integrate_static(plan.handle, BATCH, ctypes.c_void_p(got.data_ptr()), STEPS, stream)
+        assert rc == _lib.FSM_OK, _lib.last_error()
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before, (free_before, free_after)
+
+
 def test_static_entry_rejects_work_above_the_array():
     lib = _lib.load()
     op, plan, state0 = _plan_and_state()

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -645,12 +646,26 @@ int split_parts(const FsmPlan* p, int batch) {
 namespace {
 using fsm::kMaxParts;
 
-// kMaxParts non-blocking streams per (device, caller stream), created once, with the
-// caller's priority, for the parts of a split batch.
-static std::mutex g_split_mutex;
-static std::map<std::pair<int, cudaStream_t>, std::vector<cudaStream_t>> g_split;
+// kMaxParts non-blocking streams per (device, caller stream), with the caller's priority, for
+// the parts of a split batch. The sets of the kSplitCallers most recently used caller streams
+// are kept; an older set is released when the last call using it returns (cudaStreamDestroy
+// lets work already queued on a stream finish), so callers that create and drop streams do not
+// accumulate library streams.
+constexpr size_t kSplitCallers = 32;
 
-int split_streams(cudaStream_t st, cudaStream_t* out) {
+struct SplitStreams {
+  cudaStream_t s[kMaxParts] = {};
+  int n = 0;
+  ~SplitStreams() {
+    for (int h = 0; h < n; ++h) cudaStreamDestroy(s[h]);
+  }
+};
+
+static std::mutex g_split_mutex;
+static std::map<std::pair<int, cudaStream_t>, std::pair<std::shared_ptr<SplitStreams>, uint64_t>> g_split;
+static uint64_t g_split_clock = 0;
+
+int split_streams(cudaStream_t st, std::shared_ptr<SplitStreams>* out) {
   int dev = 0;
   int rc = cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
   if (rc) return rc;
@@ -659,14 +674,39 @@ int split_streams(cudaStream_t st, cudaStream_t* out) {
   if (it == g_split.end()) {
     int prio = 0;
     if ((rc = cuda_check(cudaStreamGetPriority(st, &prio), "cudaStreamGetPriority"))) return rc;
-    std::vector<cudaStream_t> v(kMaxParts);
-    for (auto& sv : v)
-      if ((rc = cuda_check(cudaStreamCreateWithPriority(&sv, cudaStreamNonBlocking, prio), "stream"))) return rc;
-    it = g_split.emplace(std::make_pair(dev, st), v).first;
+    auto set = std::make_shared<SplitStreams>();
+    for (; set->n < kMaxParts; ++set->n)
+      if ((rc = cuda_check(cudaStreamCreateWithPriority(&set->s[set->n], cudaStreamNonBlocking, prio), "stream")))
+        return rc;  // the streams created so far are destroyed with the set
+    if (g_split.size() >= kSplitCallers) {  // drop the least recently used caller's set
+      auto old = g_split.begin();
+      for (auto j = g_split.begin(); j != g_split.end(); ++j)
+        if (j->second.second < old->second.second) old = j;
+      g_split.erase(old);
+    }
+    it = g_split.emplace(std::make_pair(dev, st), std::make_pair(set, (uint64_t)0)).first;
   }
-  for (int h = 0; h < kMaxParts; ++h) out[h] = it->second[h];
+  it->second.second = ++g_split_clock;
+  *out = it->second.first;
   return FSM_OK;
 }
+
+// Events of one split integrate, destroyed on every return path (a destroyed event that is still
+// recorded on a stream is released once the stream has passed it).
+struct SplitEvents {
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t done[kMaxParts] = {};
+  ~SplitEvents() {
+    if (fork) cudaEventDestroy(fork);
+    for (int h = 0; h < kMaxParts; ++h)
+      if (done[h]) cudaEventDestroy(done[h]);
+  }
+  int create(int np) {
+    int rc = cuda_check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event");
+    for (int h = 0; h < np && !rc; ++h) rc = cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "event");
+    return rc;
+  }
+};
 
 // The arguments of samples [b0, b0 + n) of a batch: state, trajectory, per-sample tables and
 // sources offset to the first sample, the pass arrays laid out for n samples in their own
@@ -750,7 +790,15 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   char* ws = (char*)workspace;
   int32_t* d_slots = (int32_t*)ws;
   int rc;
-  if (record_slot) {
+  // The line (1D) and pointwise kernels read the record slots from the device; the plane and
+  // volume passes take them per launch from the host array. The copy reads the caller's host
+  // array when it runs, so a captured graph would read it again at every replay: recording is
+  // refused while the stream is being captured.
+  if (record_slot && (p->path == 1 || p->path == 3)) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if ((rc = cuda_check(cudaStreamIsCapturing(st, &cs), "stream capture query"))) return rc;
+    if (cs != cudaStreamCaptureStatusNone)
+      return set_error(FSM_ERR_INVALID, "integrate: recording is not supported while the stream is being captured");
     if ((rc = cuda_check(cudaMemcpyAsync(d_slots, record_slot, (size_t)(steps + 1) * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, st), "copy record slots")))
       return rc;
@@ -817,12 +865,13 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   }
   // The parts are enqueued step by step, each part's step waiting for the previous step of
   // the part before it (a ring), so that none runs ahead and leaves the others alone at the end.
-  cudaStream_t sub[kMaxParts];
-  if ((rc = split_streams(st, sub))) return rc;
-  cudaEvent_t fork, done[kMaxParts];
-  if ((rc = cuda_check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "event"))) return rc;
-  for (int h = 0; h < NP; ++h)
-    if ((rc = cuda_check(cudaEventCreateWithFlags(&done[h], cudaEventDisableTiming), "event"))) return rc;
+  std::shared_ptr<SplitStreams> streams;
+  if ((rc = split_streams(st, &streams))) return rc;
+  const cudaStream_t* sub = streams->s;
+  SplitEvents ev;
+  if ((rc = ev.create(NP))) return rc;
+  const cudaEvent_t fork = ev.fork;
+  const cudaEvent_t* done = ev.done;
   PlaneSequence q[kMaxParts];
   for (int h = 0; h < NP; ++h) {
     const int b0 = (int)((int64_t)batch * h / NP), b1 = (int)((int64_t)batch * (h + 1) / NP);
@@ -842,8 +891,6 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
     for (int h = 0; h < NP && !rc; ++h) rc = cuda_check(cudaEventRecord(done[h], sub[h]), "step event");
   }
   for (int h = 0; h < NP && !rc; ++h) rc = cuda_check(cudaStreamWaitEvent(st, done[h], 0), "join wait");
-  cudaEventDestroy(fork);  // released once the recorded work completes
-  for (int h = 0; h < NP; ++h) cudaEventDestroy(done[h]);
   return rc;
 }
 

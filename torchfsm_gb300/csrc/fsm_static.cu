@@ -22,7 +22,8 @@ void* g_scratch_addr[kMaxDevices] = {};
 // Device address of the scratch array on the current device. The host-side
 // name g_static_scratch is only a stand-in for the symbol, never a usable
 // pointer: the address is looked up once per device, with that device
-// current, and cached.
+// current, and cached for the life of the process (a device reset after the
+// first call would leave the cached address stale; resets are not supported).
 int scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

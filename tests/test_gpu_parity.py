@@ -24,7 +24,7 @@ SUPPORTED = sorted(C.CASES)
 
 
 def _run(name, device="cuda", dtype=torch.float32):
-    case = C.CASES[name]
+    case = C._case(name)
     M = C.namespace("torchfsm_gb300")
     op = case["build"](M)
     if case.get("integrator"):

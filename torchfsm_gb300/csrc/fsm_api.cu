@@ -430,6 +430,16 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
       }
     }
   }
+  p->hk = p->h;
+  if (path == 2) {
+    const int n0 = mesh->n[0], n1 = mesh->n[1];
+    const bool reg = is_pow2(n0) && n0 >= 16 && n0 <= 256 && is_pow2(n1) && n1 >= 16 && n1 <= 256;
+    int pre = 0;
+    while (pre < p->h && keep[p->koff[1] + pre]) ++pre;
+    bool prefix = true;
+    for (int j = pre; j < p->h; ++j) prefix = prefix && !keep[p->koff[1] + j];
+    if (reg && prefix && pre == n1 / 3 + 1) p->hk = pre;
+  }
   std::vector<float2> tw(kTwiddleMax);
   for (int k = 0; k < kTwiddleMax; ++k) {
     const double ang = 2.0 * M_PI * (double)k / (double)kTwiddleMax;
@@ -823,6 +833,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.keepy = p->keep + p->koff[p->ndim - 1];
   a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
   a.tile_zero = p->tile_zero;
+  a.hk = p->hk;
   a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
   a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));

@@ -333,6 +333,11 @@ struct FsmPlan {
   // per column tile of the register axis-0 pass (W adjacent inner columns): 1 where every column
   // is dealiased, so that the next-stage fields built there are zero (null: no such pass)
   uint8_t* tile_zero = nullptr;
+  // 2D plane passes: the leading last-axis columns of the stage fields that the row pass reads.
+  // Below h when the dealias mask keeps the prefix of n1/3 + 1 columns (the 2/3 rule) and the
+  // register passes run both axes: the fields beyond it are zero, so the column pass does not
+  // store them and the row pass does not load them.
+  int hk = 0;
 };
 
 namespace fsm {

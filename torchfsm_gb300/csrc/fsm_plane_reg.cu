@@ -242,6 +242,8 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
       axis0_update<NX, KIND, DIM, -1, -1>(a, tileA, b, c0, cg, last);
     }
     if (!a.emit) continue;  // uniform: no further barriers in this group
+    // 2D: columns from hk on are dealiased and the row pass does not read them: nothing to store
+    if (c0 >= ((DIM == 2) ? (int64_t)a.hk : inner)) continue;  // uniform
     if (a.tile_zero && a.tile_zero[blockIdx.x]) {
       // every column of this tile is dealiased: the next-stage fields are zero here, written
       // directly (coalesced rows of W columns) without the transforms
@@ -299,7 +301,7 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
       for (int it = 0; it < NX * W / 256; ++it) {
         const int idx = threadIdx.x + it * 256;
         const int row = idx / W, cc = idx % W;
-        if (c0 + cc < inner) dst[(int64_t)row * inner + c0 + cc] = tileB[cc * P + row];
+        if (c0 + cc < ((DIM == 2) ? (int64_t)a.hk : inner)) dst[(int64_t)row * inner + c0 + cc] = tileB[cc * P + row];
       }
       __syncthreads();
     }
@@ -350,7 +352,21 @@ __device__ __forceinline__ void split_store_r(const float2 (&zp)[RegShape<NY>::E
   }
 }
 
-template <int NY, int KIND>
+// Whether every lane of register j (indices k = t + T j, folded to kk = min(k, NY - k)) lies at
+// or beyond the kept prefix HK of the last axis: such registers hold zeros and load nothing.
+template <int NY, int T, int HK>
+__device__ __forceinline__ constexpr bool reg_dead(int j) {
+  int mn = NY;
+  for (int t = 0; t < T; ++t) {
+    const int k = t + T * j;
+    const int kk = k <= NY / 2 ? k : NY - k;
+    mn = kk < mn ? kk : mn;
+  }
+  return mn >= HK;
+}
+
+// HK: the stage fields' stored columns (FsmPlan::hk), NY/2 + 1 when every column is stored.
+template <int NY, int KIND, int HK>
 __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
   using Cfg = RowCfgR<NY>;
   constexpr int T = Cfg::T, E = Cfg::E, SCR = Cfg::SCR;
@@ -370,6 +386,7 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
   const float2* mid = a.mid + (int64_t)b * a.n_mid * S;
   float2* prod = a.prod + (int64_t)b * a.n_prod * S;
 
+  const float2 zero = make_float2(0.f, 0.f);
   if (KIND == FSM_NL_VORTICITY || KIND == FSM_NL_KS) {
     float p[2][E];
 #pragma unroll
@@ -378,19 +395,25 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
       float2 Z1[E], Z2[E];
 #pragma unroll
       for (int j = 0; j < E; ++j) {
+        if (reg_dead<NY, T, HK>(j)) {
+          Z1[j] = zero;
+          Z2[j] = zero;
+          continue;
+        }
         const int k = t + T * j;
         const bool hi = k > NY / 2;
         const int kk = hi ? NY - k : k;
         const bool selfc = (kk == 0) || (kk == NY / 2);
+        const bool live = HK > NY / 2 || kk < HK;
         const float kyv = ky[kk];
         if (KIND == FSM_NL_VORTICITY) {
-          const float2 m0 = mid[roff + kk], m1 = mid[S + roff + kk];
-          const float2 m2 = mid[2 * S + roff + kk], m3 = mid[3 * S + roff + kk];
+          const float2 m0 = live ? mid[roff + kk] : zero, m1 = live ? mid[S + roff + kk] : zero;
+          const float2 m2 = live ? mid[2 * S + roff + kk] : zero, m3 = live ? mid[3 * S + roff + kk] : zero;
           // u_x + i u_y with u_x <- i ky psi, u_y <- -(i kx psi); w_x + i w_y with w_x <- i kx w, w_y <- i ky w
           Z1[j] = herm_z(cscale(cmuli(m0), kyv), make_float2(-m1.x, -m1.y), selfc, hi);
           Z2[j] = herm_z(m3, cscale(cmuli(m2), kyv), selfc, hi);
         } else {
-          const float2 m0 = mid[roff + kk], m1 = mid[S + roff + kk];
+          const float2 m0 = live ? mid[roff + kk] : zero, m1 = live ? mid[S + roff + kk] : zero;
           Z1[j] = herm_z(m1, cscale(cmuli(m0), kyv), selfc, hi);  // phi_x + i phi_y
         }
       }
@@ -417,12 +440,18 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
       float2 Z1[E], Z2[E];
 #pragma unroll
       for (int j = 0; j < E; ++j) {
+        if (reg_dead<NY, T, HK>(j)) {
+          Z1[j] = zero;
+          Z2[j] = zero;
+          continue;
+        }
         const int k = t + T * j;
         const bool hi = k > NY / 2;
         const int kk = hi ? NY - k : k;
         const bool selfc = (kk == 0) || (kk == NY / 2);
-        Z1[j] = herm_z(mid[roff + kk], mid[2 * S + roff + kk], selfc, hi);          // u0 + i u1
-        Z2[j] = herm_z(mid[S + roff + kk], mid[3 * S + roff + kk], selfc, hi);      // dx u0 + i dx u1
+        const bool live = HK > NY / 2 || kk < HK;
+        Z1[j] = live ? herm_z(mid[roff + kk], mid[2 * S + roff + kk], selfc, hi) : zero;       // u0 + i u1
+        Z2[j] = live ? herm_z(mid[S + roff + kk], mid[3 * S + roff + kk], selfc, hi) : zero;   // dx u0 + i dx u1
       }
       reg_fft<NY, true>(Z1, scr, twt, t);
       reg_fft<NY, true>(Z2, scr, twt, t);
@@ -435,12 +464,18 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
       }
 #pragma unroll
       for (int j = 0; j < E; ++j) {
+        if (reg_dead<NY, T, HK>(j)) {
+          Z2[j] = zero;
+          continue;
+        }
         const int k = t + T * j;
         const bool hi = k > NY / 2;
         const int kk = hi ? NY - k : k;
         const bool selfc = (kk == 0) || (kk == NY / 2);
+        const bool live = HK > NY / 2 || kk < HK;
         const float kyv = ky[kk];
-        Z2[j] = herm_z(cscale(cmuli(mid[roff + kk]), kyv), cscale(cmuli(mid[2 * S + roff + kk]), kyv), selfc, hi);
+        Z2[j] = live ? herm_z(cscale(cmuli(mid[roff + kk]), kyv), cscale(cmuli(mid[2 * S + roff + kk]), kyv), selfc, hi)
+                     : zero;
       }
       reg_fft<NY, true>(Z2, scr, twt, t);  // dy u0 + i dy u1
 #pragma unroll
@@ -467,19 +502,27 @@ static int launch_axis0_r(const StepArgs& a, cudaStream_t st) {
   return cuda_check(cudaGetLastError(), "k_axis0_r");
 }
 
-template <int NY, int KIND>
-static int launch_row_r(int nx, const StepArgs& a, cudaStream_t st) {
+template <int NY, int KIND, int HK>
+static int launch_row_r_hk(int nx, const StepArgs& a, cudaStream_t st) {
   using Cfg = RowCfgR<NY>;
   const int groups_needed = nx / 2;
   int threads = groups_needed * Cfg::T;
   if (threads > 256) threads = 256;
   const int groups = threads / Cfg::T;
   const size_t smem = (size_t)(NY + groups * Cfg::SCR) * sizeof(float2);
-  int rc = prep_smem(k_plane_row_r<NY, KIND>, smem);
+  int rc = prep_smem(k_plane_row_r<NY, KIND, HK>, smem);
   if (rc) return rc;
   dim3 grid(groups_needed / groups, a.B);
-  k_plane_row_r<NY, KIND><<<grid, threads, smem, st>>>(a);
+  k_plane_row_r<NY, KIND, HK><<<grid, threads, smem, st>>>(a);
   return cuda_check(cudaGetLastError(), "k_plane_row_r");
+}
+
+// The 2/3 rule's stored prefix (NY/3 + 1 columns) or every column.
+template <int NY, int KIND>
+static int launch_row_r(int nx, const StepArgs& a, cudaStream_t st) {
+  if (a.hk == NY / 3 + 1) return launch_row_r_hk<NY, KIND, NY / 3 + 1>(nx, a, st);
+  if (a.hk != NY / 2 + 1) return set_error(FSM_ERR_INVALID, "row pass: unexpected stored column count");
+  return launch_row_r_hk<NY, KIND, NY / 2 + 1>(nx, a, st);
 }
 
 template <int KIND, int DIM>

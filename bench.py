@@ -727,7 +727,7 @@ def run_burgers1d(args):
             "cpu_baseline": {"value": n * steps / cpu_s, "unit": "DOF*steps/s", "cores": 1, "kind": "port",
                              "sample": "the whole workload, numpy complex64 restatement, 1 thread"},
             "torch_gpu_reference": torch_ref}
-    print(json.dumps(line))
+    return line
 
 
 def run_burgers3d(args):
@@ -815,7 +815,7 @@ def run_burgers3d(args):
                          "step_achieved_gbs": 276.0 * dof_steps / (ms * 1e-3) / 1e9, "peak": _peaks()[0]},
             "torch_gpu_reference": torch_ref,
             "clocks": clk.summary()}
-    print(json.dumps(line))
+    return line
 
 
 def run_serving(args):
@@ -992,7 +992,7 @@ def run_burgers2d_grad(args):
                           "rel_diff_vs_richardson": abs(gnu - fd) / abs(fd),
                           "grad_u0_finite": bool(torch.isfinite(gu).all())},
             "reference_autograd": ref}
-    print(json.dumps(line))
+    return line
 
 
 def reference_autograd_burgers2d(device, u0h, target, mesh, dt, steps) -> dict:
@@ -1072,6 +1072,52 @@ def ncu_case(workload: str = "ns2d", n3d: int = 256):
     print("ncu case done", bool(torch.isfinite(out).all().item()))
 
 
+def _summary(line: dict, keys) -> dict:
+    out = {}
+    for k in keys:
+        cur, src = line, k.split(".")
+        for part in src:
+            cur = cur.get(part) if isinstance(cur, dict) else None
+        out[k] = cur
+    return out
+
+
+def other_workloads(args) -> dict:
+    """The other named workloads, run after the headline's timed region and summarised on its line:
+    1D Burgers N=128 solve latency, 3D Burgers 256^3 throughput with its FP64 error after 50 steps,
+    and the differentiable 2D Burgers forward + backward with its gradient checks. Each runs with few
+    repetitions (its own workload line, ``--workload``, has the full figures); a failure is reported
+    and leaves the headline intact."""
+    import argparse as _ap
+
+    small = _ap.Namespace(**dict(vars(args), steps=3, warmup=1))
+    legs = {
+        "burgers1d_n128_200steps": (run_burgers1d, ["value", "unit", "latency_ms", "config.rel_l2_traj_vs_fp64",
+                                                    "torch_gpu_reference.latency_ms",
+                                                    "torch_gpu_reference.fused_e2e_over_reference"]),
+        "burgers3d_256cubed_200steps": (run_burgers3d, ["value", "unit", "ms_per_step", "e2e.value",
+                                                        "config.rel_l2_vs_fp64_after_50_steps",
+                                                        "roofline.step_achieved_gbs", "roofline.per_kernel_ms",
+                                                        "torch_gpu_reference.value",
+                                                        "torch_gpu_reference.fused_device_over_reference"]),
+        "burgers2d_grad_128x128_b16_500steps": (run_burgers2d_grad, ["value", "unit", "ms_per_step", "forward_only",
+                                                                     "gradients.grad_nu_adjoint",
+                                                                     "gradients.rel_diff_vs_richardson",
+                                                                     "reference_autograd.seconds_fwd_bwd",
+                                                                     "reference_autograd.rel_l2_grad_u0_vs_adjoint",
+                                                                     "reference_autograd.rel_diff_grad_nu_vs_adjoint"]),
+    }
+    out = {}
+    for name, (fn, keys) in legs.items():
+        t0 = time.perf_counter()
+        try:
+            out[name] = _summary(fn(small), keys)
+        except Exception as e:  # noqa: BLE001 -- a summary leg must not cost the headline line
+            out[name] = {"unavailable": f"{type(e).__name__}: {e}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+    return out
+
+
 def fused_line(res: dict, args, world: int, cpu: Optional[dict], ref_cpu: Optional[dict]) -> dict:
     """The JSON line of the fused arm from ``run_fused``'s measurements and the CPU baselines."""
     dof_steps = res["B"] * N * N * TIME_STEPS
@@ -1129,6 +1175,8 @@ def main():
                     help="skip the reference torch GPU path leg of the ns2d workload")
     ap.add_argument("--ref-cpu-samples", type=int, default=8,
                     help="ns2d: samples of the batch run by the reference package on the host cores (0: skip)")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="ns2d: skip the summaries of the 1D, 3D and gradient workloads run after the timed region")
     ap.add_argument("--no-fp64-reference", action="store_true",
                     help="skip the accuracy leg (the reference's float64 run of the first samples)")
     ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
@@ -1153,16 +1201,16 @@ def main():
         ncu_case(args.workload, args.ncu_n)
         return
     if args.workload == "burgers1d" and args.impl == "fused":
-        run_burgers1d(args)
+        print(json.dumps(run_burgers1d(args)))
         return
     if args.workload == "burgers3d" and args.impl == "fused":
-        run_burgers3d(args)
+        print(json.dumps(run_burgers3d(args)))
         return
     if args.workload == "serving" and args.impl == "fused":
         run_serving(args)
         return
     if args.workload == "burgers2d_grad" and args.impl == "fused":
-        run_burgers2d_grad(args)
+        print(json.dumps(run_burgers2d_grad(args)))
         return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -1206,6 +1254,8 @@ def main():
                                    os.cpu_count() or 1) if world == 1 else None
     ref_cpu = reference_cpu_throughput(args.ref_cpu_samples) if world == 1 and args.ref_cpu_samples > 0 else None
     line = fused_line(res, args, world, cpu, ref_cpu)
+    if world == 1 and not args.no_other_workloads:
+        line["other_workloads"] = other_workloads(args)
     print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()

@@ -195,3 +195,29 @@ def test_fused_line_from_measurements():
     line2 = bench.fused_line(res2, args, 2, None, None)
     assert line2["cpu_baseline"] is None and line2["reference_cpu"] is None
     assert math.isclose(line2["value"], 2 * dof_steps / 0.25) and line2["config"]["rel_l2_vs_fp64"] is None
+
+
+def test_other_workloads_summaries_and_failures(monkeypatch):
+    """The headline line's summaries of the other workloads: the named keys of each leg's own line,
+    run with few repetitions, and a failing leg reported instead of raised."""
+    import argparse
+
+    seen = {}
+
+    def fake_1d(args):
+        seen["steps"], seen["warmup"] = args.steps, args.warmup
+        return {"value": 1.0, "unit": "DOF*steps/s", "latency_ms": {"p50": 2.0}, "config": {"rel_l2_traj_vs_fp64": 3e-7}}
+
+    def broken(args):
+        raise RuntimeError("no GPU")
+
+    monkeypatch.setattr(bench, "run_burgers1d", fake_1d)
+    monkeypatch.setattr(bench, "run_burgers3d", broken)
+    monkeypatch.setattr(bench, "run_burgers2d_grad", broken)
+    out = bench.other_workloads(argparse.Namespace(steps=20, warmup=5, no_fp64_reference=False))
+    one = out["burgers1d_n128_200steps"]
+    assert one["value"] == 1.0 and one["latency_ms"] == {"p50": 2.0} and one["config.rel_l2_traj_vs_fp64"] == 3e-7
+    assert one["torch_gpu_reference.latency_ms"] is None and one["wall_s"] >= 0
+    assert (seen["steps"], seen["warmup"]) == (3, 1)
+    assert "no GPU" in out["burgers3d_256cubed_200steps"]["unavailable"]
+    assert "no GPU" in out["burgers2d_grad_128x128_b16_500steps"]["unavailable"]

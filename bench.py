@@ -908,6 +908,7 @@ def run_serving(args):
             "e2e": {"value": serve_tp, "unit": "DOF*steps/s",
                     "h2d_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs),
                     "d2h_bytes_per_step": sum(r.u0.numel() * 4 for r in reqs)}}
+    server.close()
     print(json.dumps(line))
 
 

@@ -11,8 +11,8 @@ pytestmark = pytest.mark.gpu
 def test_results_same_alone_and_in_the_mix():
     device = torch.device("cuda", 0)
     reqs = serving.make_stream(14, seed=3, rate_hz=0.0, max_steps=150, min_steps=20)
-    server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=17)
-    server.run(reqs, realtime=False)
+    with serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=17) as server:
+        server.run(reqs, realtime=False)
     ops = {}
     for r in reqs:
         alone, _ = serving.solve_alone(r, device, ops)
@@ -25,8 +25,8 @@ def test_results_same_alone_and_in_the_mix():
 def test_threaded_loop_gives_the_same_results():
     device = torch.device("cuda", 0)
     reqs = serving.make_stream(10, seed=4, rate_hz=0.0, max_steps=120, min_steps=20)
-    server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=13)
-    server.run_threaded(reqs, realtime=False)
+    with serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=13) as server:
+        server.run_threaded(reqs, realtime=False)
     ops = {}
     for r in reqs:
         alone, _ = serving.solve_alone(r, device, ops)
@@ -37,13 +37,24 @@ def test_threaded_loop_gives_the_same_results():
 def test_admission_respects_capacity_and_compacts():
     device = torch.device("cuda", 0)
     reqs = [r for r in serving.make_stream(40, seed=5, rate_hz=0.0, max_steps=60, min_steps=10) if r.kind == "ks1d"]
-    server = serving.SolveServer(device, hbm_budget_bytes=1 << 20, chunk=9, max_slots=40)
-    server.run(reqs, realtime=False)
-    for b in server.buckets.values():
-        st = b.engine.stats()
-        assert st["occupied"] == 0 and st["waiting"] == 0 and st["active"] == 0 and not b.pending
-        assert st["completed"] == sum(1 for r in reqs if (r.kind, r.n) == (b.kind, b.n))
+    with serving.SolveServer(device, hbm_budget_bytes=1 << 20, chunk=9, max_slots=40) as server:
+        server.run(reqs, realtime=False)
+        for b in server.buckets.values():
+            st = b.engine.stats()
+            assert st["occupied"] == 0 and st["waiting"] == 0 and st["active"] == 0 and not b.pending
+            assert st["completed"] == sum(1 for r in reqs if (r.kind, r.n) == (b.kind, b.n))
     assert all(r.result is not None and r.t_done >= r.t_admit for r in reqs)
+
+
+def test_close_releases_engines_before_plans():
+    device = torch.device("cuda", 0)
+    reqs = serving.make_stream(4, seed=8, rate_hz=0.0, max_steps=40, min_steps=10)
+    server = serving.SolveServer(device, hbm_budget_bytes=1 << 28, chunk=8)
+    server.run_threaded(reqs, realtime=False)
+    buckets = list(server.buckets.values())
+    server.close()
+    assert server.buckets == {} and all(b.engine is None and b.plan is None for b in buckets)
+    assert all(r.result is not None for r in reqs)
 
 
 def test_graph_replays_match_direct_launches():
@@ -51,12 +62,12 @@ def test_graph_replays_match_direct_launches():
     out = {}
     for graphs in (False, True):
         reqs = serving.make_stream(12, seed=6, rate_hz=0.0, max_steps=90, min_steps=30)
-        server = serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=8, graphs=graphs)
-        server.run(reqs, realtime=False)
-        out[graphs] = [r.result for r in reqs]
-        if graphs:
-            assert server.graph_replays > 0
-        else:
-            assert server.graph_replays == 0
+        with serving.SolveServer(device, hbm_budget_bytes=1 << 30, chunk=8, graphs=graphs) as server:
+            server.run(reqs, realtime=False)
+            out[graphs] = [r.result for r in reqs]
+            if graphs:
+                assert server.graph_replays > 0
+            else:
+                assert server.graph_replays == 0
     for a, b in zip(out[False], out[True]):
         assert torch.equal(a, b)

@@ -25,6 +25,7 @@ The reference has no serving layer; the solves themselves follow
 from __future__ import annotations
 
 import collections
+import gc
 import math
 import threading
 import time
@@ -165,6 +166,15 @@ class _Bucket:
                 done.append(r)
         return done
 
+    def close(self) -> None:
+        """Destroy the engine (it waits for the bucket's stream), then the plan it used."""
+        if self.engine is not None:
+            self.engine.__del__()
+            self.engine = None
+        if self.plan is not None:
+            self.plan.__del__()
+            self.plan = None
+
     @property
     def idle(self) -> bool:
         st = self.engine.stats()
@@ -284,6 +294,20 @@ class SolveServer:
                 errors.append(e)
 
         threads = [threading.Thread(target=worker, args=(k,), daemon=True) for k in self.buckets]
+        # No garbage collection while the workers run: a collection triggered in one worker runs
+        # the finalizers of unreachable library objects there (plan destruction synchronises the
+        # device and frees memory), while another worker may be capturing a tick's CUDA graph on its
+        # stream. Collect before, and let the collector run again once the workers are joined.
+        gc_was_enabled = gc.isenabled()
+        gc.collect()
+        gc.disable()
+        try:
+            return self._serve_threads(threads, pending, queues, cond, state, now, realtime, errors)
+        finally:
+            if gc_was_enabled:
+                gc.enable()
+
+    def _serve_threads(self, threads, pending, queues, cond, state, now, realtime, errors) -> float:
         for th in threads:
             th.start()
         for r in pending:
@@ -302,6 +326,18 @@ class SolveServer:
         if errors:
             raise errors[0]
         return now()
+
+    def close(self) -> None:
+        """Release the buckets: each engine (it waits for its stream) before its plan."""
+        for b in self.buckets.values():
+            b.close()
+        self.buckets = {}
+
+    def __enter__(self) -> "SolveServer":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
 
     @property
     def launches(self) -> int:

@@ -108,6 +108,97 @@ __device__ __forceinline__ void nv_leray(float2 (&nv)[CG], const PointK<DIM>& pk
   for (int c = 0; c < CG; ++c) nv[c] = out[c];
 }
 
+// One SETDRK4 stage at one point from its operands already in registers (the recurrences of
+// etd_stage_c): ua is u at stages 0 and 1, acc at stages 2 and 3; ub is acc at stage 1, q at stage
+// 2. The running sums the stage writes are returned in acc / q, the new state (stage 3) in the
+// return value, which is otherwise the next stage's input.
+template <int S>
+__device__ __forceinline__ float2 setdrk4_pre(float2 nv, float2 ua, float2 ub, const float2* __restrict__ tab,
+                                              int64_t ts, float2& acc, float2& q) {
+  if (S == 0) {
+    const float2 Em1 = tab[0], E2m1 = tab[ts], c1 = tab[2 * ts], c4 = tab[3 * ts];
+    const float2 a1 = cfma(c1, nv, cexpmul(E2m1, ua));
+    acc = cfma(c4, nv, cexpmul(Em1, ua));
+    q = cfma(make_float2(-c1.x, -c1.y), nv, cexpmul(E2m1, a1));
+    return a1;
+  } else if (S == 1) {
+    const float2 E2m1 = tab[ts], c1 = tab[2 * ts], c5 = tab[4 * ts];
+    acc = cfma(cscale(c5, 2.f), nv, ub);
+    return cfma(c1, nv, cexpmul(E2m1, ua));
+  } else if (S == 2) {
+    const float2 c1 = tab[2 * ts], c5 = tab[4 * ts];
+    acc = cfma(cscale(c5, 2.f), nv, ua);
+    return cfma(cscale(c1, 2.f), nv, ub);
+  } else {
+    return cfma(tab[5 * ts], nv, ua);
+  }
+}
+
+// Phase 2 of k_axis0_r for SETDRK4 stages of one-channel groups: the state operands the thread's
+// points need from HBM (u at stages 0 and 1, acc at 1, 2 and 3, q at 2) are loaded first for a
+// group of points, in one round, then those points are updated with their table loads (which hit
+// L2). Loading them four points at a time left four rounds of HBM latency in each CTA's critical
+// path (on 2D vorticity 256^2 x 64 the column pass went from 55 to 43 us per launch).
+template <int NX, int KIND, int DIM, int STG>
+__device__ __forceinline__ void axis0_update_hoisted(const StepArgs& a, float2* __restrict__ tileA, int b, int64_t c0,
+                                                     int cg, bool last) {
+  using Cfg = ColCfg<NX>;
+  using K = RegKind<KIND, DIM>;
+  constexpr int W = Cfg::W, P = Cfg::P, C = K::C;
+  constexpr int PPT = NX * W / 256, RSTEP = 256 / W;
+  const int64_t S = a.S;
+  const int64_t inner = S / NX;
+  const int col = threadIdx.x % W, row0 = threadIdx.x / W;
+  const int64_t j = c0 + col;
+  if (j >= inner) return;
+  const int c = cg;
+  float2* __restrict__ up = a.state + ((int64_t)b * C + c) * S + j;
+  float2* __restrict__ accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + j;
+  float2* __restrict__ qp = a.aux + ((int64_t)b * a.n_aux * C + C + c) * S + j;
+  const float2* __restrict__ tab = a.tab + ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + j;
+  const float2* __restrict__ srcp =
+      a.src ? a.src + ((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + j : nullptr;
+  const float2* __restrict__ o1p = (STG <= 1) ? up : accp;
+  const float2* __restrict__ o2p = (STG == 1) ? accp : qp;
+  // operands of HALF points at a time, one HBM round per group: eight points (vorticity) and four
+  // (convection, whose kernel holds more) keep the kernels inside two CTAs' registers per SM
+  constexpr int HMAX = (KIND == FSM_NL_CONVECTION) ? 4 : 8;
+  constexpr int HALF = PPT > HMAX ? HMAX : PPT;
+#pragma unroll 1
+  for (int h0 = 0; h0 < PPT; h0 += HALF) {
+  float2 o1[HALF], o2[HALF];
+#pragma unroll
+  for (int ih = 0; ih < HALF; ++ih) {
+    const int64_t r = (int64_t)(row0 + RSTEP * (h0 + ih)) * inner;
+    o1[ih] = o1p[r];
+    if (STG == 1 || STG == 2) o2[ih] = o2p[r];
+  }
+#pragma unroll
+  for (int ih = 0; ih < HALF; ++ih) {
+    const int it = h0 + ih;
+    // the table loads of four points at a time: without this fence the compiler issues those of
+    // every point at once, beside the operands, and runs out of registers
+    
+    const int row = row0 + RSTEP * it;
+    const int64_t r = (int64_t)row * inner;
+    const PointK<DIM> pk = point_k<DIM>(a, row, j);
+    float2 nv = tileA[col * P + row];
+    if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && row == 0 && j == 0) nv = csub(nv, a.dc[0]);
+    nv = cscale(nv, a.coef);
+    if (srcp) nv = cadd(nv, srcp[r]);
+    float2 acc, q;
+    const float2 st = setdrk4_pre<STG>(nv, o1[ih], (STG == 1 || STG == 2) ? o2[ih] : o1[ih], tab + r, a.ts, acc, q);
+    if (STG <= 2) accp[r] = acc;
+    if (STG == 0) qp[r] = q;
+    if (STG == 3) {
+      up[r] = st;
+      if (a.slot >= 0 && last) a.traj[(((int64_t)b * a.n_frames + a.slot) * C + c) * S + r + j] = st;
+    }
+    tileA[col * P + row] = cscale(st, pk.mask);
+  }
+  }
+}
+
 // Phase 2 of k_axis0_r: the stage update at every point of the tile, in a coalesced point
 // mapping, leaving the masked next-stage field in tileA. INTEG/STG name the scheme and stage
 // at compile time (so that the loads of several points are issued together); -1 dispatches
@@ -177,8 +268,10 @@ __device__ __forceinline__ void axis0_update(const StepArgs& a, float2* __restri
 //   2. stage update at every point, recording when a step completes
 //   3. next stage field (mask, 1/N, i kx, streamfunction) -> inverse transform -> mid fields
 // Channels are processed in groups so that Convection needs one staging tile.
-template <int NX, int KIND, int DIM>
-__global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
+// FAST: a SETDRK4 stage launch of a vorticity or convection program (channel groups of one
+// channel; the hoisted update, two CTAs per SM); otherwise any scheme, the priming launch included.
+template <int NX, int KIND, int DIM, bool FAST>
+__global__ void __launch_bounds__(256, FAST ? 2 : 1) k_axis0_r(StepArgs a) {
   using Cfg = ColCfg<NX>;
   using K = RegKind<KIND, DIM>;
   constexpr int T = Cfg::T, E = Cfg::E, W = Cfg::W, P = Cfg::P, C = K::C, CG = K::CG;
@@ -231,7 +324,14 @@ __global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
     }
     __syncthreads();
 
-    if (a.stage >= 0 && a.integ == FSM_SETDRK4) {
+    if constexpr (FAST) {
+      switch (a.stage) {
+        case 0: axis0_update_hoisted<NX, KIND, DIM, 0>(a, tileA, b, c0, cg, last); break;
+        case 1: axis0_update_hoisted<NX, KIND, DIM, 1>(a, tileA, b, c0, cg, last); break;
+        case 2: axis0_update_hoisted<NX, KIND, DIM, 2>(a, tileA, b, c0, cg, last); break;
+        default: axis0_update_hoisted<NX, KIND, DIM, 3>(a, tileA, b, c0, cg, last); break;
+      }
+    } else if (a.stage >= 0 && a.integ == FSM_SETDRK4) {
       switch (a.stage) {
         case 0: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 0>(a, tileA, b, c0, cg, last); break;
         case 1: axis0_update<NX, KIND, DIM, FSM_SETDRK4, 1>(a, tileA, b, c0, cg, last); break;
@@ -489,17 +589,26 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
   }
 }
 
-template <int NX, int KIND, int DIM>
-static int launch_axis0_r(const StepArgs& a, cudaStream_t st) {
+template <int NX, int KIND, int DIM, bool FAST>
+static int launch_axis0_r_mode(const StepArgs& a, cudaStream_t st) {
   using Cfg = ColCfg<NX>;
   using K = RegKind<KIND, DIM>;
   const size_t smem = (size_t)(NX + (K::CG + 1) * Cfg::W * Cfg::P) * sizeof(float2);
-  int rc = prep_smem(k_axis0_r<NX, KIND, DIM>, smem);
+  int rc = prep_smem(k_axis0_r<NX, KIND, DIM, FAST>, smem);
   if (rc) return rc;
   const int64_t inner = a.S / NX;
   dim3 grid((unsigned)((inner + Cfg::W - 1) / Cfg::W), a.B);
-  k_axis0_r<NX, KIND, DIM><<<grid, 256, smem, st>>>(a);
+  k_axis0_r<NX, KIND, DIM, FAST><<<grid, 256, smem, st>>>(a);
   return cuda_check(cudaGetLastError(), "k_axis0_r");
+}
+
+template <int NX, int KIND, int DIM>
+static int launch_axis0_r(const StepArgs& a, cudaStream_t st) {
+  // the hoisted update for vorticity and convection (KS keeps the generic kernel: its hoisted
+  // instance does not fit two CTAs' registers per SM)
+  constexpr bool fast = RegKind<KIND, DIM>::CG == 1 && KIND != FSM_NL_KS;
+  if (fast && a.integ == FSM_SETDRK4 && a.stage >= 0) return launch_axis0_r_mode<NX, KIND, DIM, fast>(a, st);
+  return launch_axis0_r_mode<NX, KIND, DIM, false>(a, st);
 }
 
 template <int NY, int KIND, int HK>

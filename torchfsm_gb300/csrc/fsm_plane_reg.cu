@@ -269,9 +269,10 @@ __device__ __forceinline__ void axis0_update(const StepArgs& a, float2* __restri
 //   3. next stage field (mask, 1/N, i kx, streamfunction) -> inverse transform -> mid fields
 // Channels are processed in groups so that Convection needs one staging tile.
 // FAST: a SETDRK4 stage launch of a vorticity or convection program (channel groups of one
-// channel; the hoisted update, two CTAs per SM); otherwise any scheme, the priming launch included.
+// channel; the hoisted update, two CTAs per SM, k_axis0_r2); otherwise any scheme, the priming
+// launch included (k_axis0_r).
 template <int NX, int KIND, int DIM, bool FAST>
-__global__ void __launch_bounds__(256, FAST ? 2 : 1) k_axis0_r(StepArgs a) {
+__device__ __forceinline__ void axis0_body(const StepArgs& a) {
   using Cfg = ColCfg<NX>;
   using K = RegKind<KIND, DIM>;
   constexpr int T = Cfg::T, E = Cfg::E, W = Cfg::W, P = Cfg::P, C = K::C, CG = K::CG;
@@ -406,6 +407,16 @@ __global__ void __launch_bounds__(256, FAST ? 2 : 1) k_axis0_r(StepArgs a) {
       __syncthreads();
     }
   }
+}
+
+template <int NX, int KIND, int DIM>
+__global__ void __launch_bounds__(256) k_axis0_r(StepArgs a) {
+  axis0_body<NX, KIND, DIM, false>(a);
+}
+
+template <int NX, int KIND, int DIM>
+__global__ void __launch_bounds__(256, 2) k_axis0_r2(StepArgs a) {
+  axis0_body<NX, KIND, DIM, true>(a);
 }
 
 template <int NY>
@@ -594,12 +605,19 @@ static int launch_axis0_r_mode(const StepArgs& a, cudaStream_t st) {
   using Cfg = ColCfg<NX>;
   using K = RegKind<KIND, DIM>;
   const size_t smem = (size_t)(NX + (K::CG + 1) * Cfg::W * Cfg::P) * sizeof(float2);
-  int rc = prep_smem(k_axis0_r<NX, KIND, DIM, FAST>, smem);
-  if (rc) return rc;
   const int64_t inner = a.S / NX;
   dim3 grid((unsigned)((inner + Cfg::W - 1) / Cfg::W), a.B);
-  k_axis0_r<NX, KIND, DIM, FAST><<<grid, 256, smem, st>>>(a);
-  return cuda_check(cudaGetLastError(), "k_axis0_r");
+  if constexpr (FAST) {
+    int rc = prep_smem(k_axis0_r2<NX, KIND, DIM>, smem);
+    if (rc) return rc;
+    k_axis0_r2<NX, KIND, DIM><<<grid, 256, smem, st>>>(a);
+    return cuda_check(cudaGetLastError(), "k_axis0_r2");
+  } else {
+    int rc = prep_smem(k_axis0_r<NX, KIND, DIM>, smem);
+    if (rc) return rc;
+    k_axis0_r<NX, KIND, DIM><<<grid, 256, smem, st>>>(a);
+    return cuda_check(cudaGetLastError(), "k_axis0_r");
+  }
 }
 
 template <int NX, int KIND, int DIM>

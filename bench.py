@@ -1065,6 +1065,35 @@ def ncu_case(workload: str = "ns2d", n3d: int = 256):
         torch.cuda.synchronize()
         print("ncu case done", bool(torch.isfinite(u.grad).all().item()))
         return
+    if workload in ("burgers1d", "ks1d", "heat2d"):
+        # the kernels outside the plane and volume passes, on small cases of their workloads:
+        # burgers1d: the 1D line kernel at N = 128 (200 steps, 201 frames), the FP64 coefficient kernel
+        # and the last-axis transforms; ks1d: the line kernel at N = 4096 (batch 32, 100 steps) and the
+        # KS batch-mean kernels (KuramotoSivashinskyHighDim in 1D, N = 1024, batch 8, 50 steps); heat2d:
+        # the pointwise kernel of a linear program and the 2D transforms at 256^2 x 64
+        from torchfsm_gb300.operator import Laplacian
+        from torchfsm_gb300.traj_recorder import AutoRecorder
+
+        device = torch.device("cuda", 0)
+        if workload == "burgers1d":
+            x = np.arange(128) / 128
+            u = torch.tensor((np.sin(2 * np.pi * x) + 0.5).reshape(1, 1, 128), dtype=torch.float32, device=device)
+            out = pde.Burgers(0.01).integrate(u_0=u, mesh=[(0.0, 1.0, 128)], dt=0.01, step=200,
+                                              trajectory_recorder=AutoRecorder())
+        elif workload == "ks1d":
+            L = 32 * math.pi
+            u = torch.tensor(initial.band_limited((4096,), 32, 1, 8, SEED, 1.0).astype(np.float32), device=device)
+            out = pde.KuramotoSivashinsky().integrate(u_0=u, mesh=[(0.0, L, 4096)], dt=0.02, step=100)
+            v = torch.tensor(initial.band_limited((1024,), 8, 1, 8, SEED, 0.7).astype(np.float32), device=device)
+            out2 = pde.KuramotoSivashinskyHighDim().integrate(u_0=v, mesh=[(0.0, 10 * math.pi, 1024)], dt=0.02,
+                                                              step=50)
+            out = torch.cat([out.flatten(), out2.flatten()])
+        else:
+            u = torch.tensor(initial_vorticity(BATCH), device=device)
+            out = (0.05 * Laplacian()).integrate(u_0=u, mesh=MESH, dt=1e-3, step=100)
+        torch.cuda.synchronize()
+        print("ncu case done", bool(torch.isfinite(out).all().item()))
+        return
     if workload == "burgers3d":
         n = n3d
         device = torch.device("cuda", 0)
@@ -1218,9 +1247,9 @@ def main():
     ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],
                     help="serving: buckets on the high-priority streams")
     ap.add_argument("--workload", default="ns2d",
-                    choices=["ns2d", "burgers1d", "burgers3d", "serving", "burgers2d_grad"],
+                    choices=["ns2d", "burgers1d", "burgers3d", "serving", "burgers2d_grad", "ks1d", "heat2d"],
                     help="ns2d: the headline (2D NS vorticity 256^2 x 64); burgers1d: 1D Burgers N=128 latency; "
-                         "burgers3d: 3D Burgers 256^3")
+                         "burgers3d: 3D Burgers 256^3; ks1d, heat2d: --ncu-case only")
     ap.add_argument("--ncu-case", action="store_true",
                     help="small profiling case: one warm-up step, then 3 time steps of the full batch")
     ap.add_argument("--ncu-n", type=int, default=256, help="grid size of the burgers3d profiling case")
@@ -1228,6 +1257,8 @@ def main():
     if args.ncu_case:
         ncu_case(args.workload, args.ncu_n)
         return
+    if args.workload in ("ks1d", "heat2d"):
+        ap.error(f"--workload {args.workload} is a profiling case: use it with --ncu-case")
     if args.workload == "burgers1d" and args.impl == "fused":
         print(json.dumps(run_burgers1d(args)))
         return

@@ -427,6 +427,34 @@ GRAD_CASES = {
 }
 
 
+# Differentiable programs the hand-written Convection adjoint does not cover (their gradients come
+# from segments recomputed in torch arithmetic and differentiated by autograd): vorticity NS, the
+# high-dimensional KS (batch-wide mean), KdV (complex symbol). build(M, coef) makes the operator with
+# the tensor coefficient ``coef`` on its first linear term; the target is the run with coef_target.
+GENERIC_GRAD_CASES = {
+    "grad_ns2d_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=1, dt=0.01, step=20, coef=0.01,
+        coef_target=0.02, ic=_grf2(301, 32),
+        build=lambda M, c: c * M.operator.Laplacian() - M.operator.VorticityConvection(),
+    ),
+    "grad_ksnd2d_n32": dict(
+        mesh=[(0, 10 * math.pi, 32), (0, 10 * math.pi, 32)], batch=2, channels=1, dt=0.02, step=15, coef=-1.0,
+        coef_target=-1.2, ic=_bl(302, (32, 32), 4, 0.5),
+        build=lambda M, c: c * M.operator.Laplacian() - M.operator.Biharmonic() - M.operator.KSConvection(),
+    ),
+    "grad_kdv1d_n64": dict(
+        mesh=[(0, 20.0, 64)], batch=2, channels=1, dt=1e-3, step=30, coef=-1.0, coef_target=-1.1,
+        ic=_bl(303, (64,), 4, 0.5),
+        build=lambda M, c: c * M.operator.SpatialDerivative(0, 3) + 6.0 * M.operator.Convection(),
+    ),
+}
+
+
+def generic_grad_initial_condition(name: str) -> np.ndarray:
+    c = GENERIC_GRAD_CASES[name]
+    return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)
+
+
 def grad_initial_condition(name: str) -> np.ndarray:
     c = GRAD_CASES[name]
     return np.ascontiguousarray(c["ic"](c["mesh"], c["batch"], c["channels"]), dtype=np.float64)

@@ -116,6 +116,23 @@ def main(ref_root: str) -> None:
                             loss=np.array(loss.item()), grad_u0=x.grad.numpy(), grad_nu=np.array(nu.grad.item()))
         print(name, "loss", loss.item(), "grad_nu", nu.grad.item())
 
+    # Gradients of the other differentiable programs by the reference's autograd (float64).
+    for name, case in C.GENERIC_GRAD_CASES.items():
+        if only and name not in only:
+            continue
+        u0 = torch.tensor(C.generic_grad_initial_condition(name), dtype=torch.float64)
+        with torch.no_grad():
+            target = case["build"](M, case["coef_target"]).integrate(u_0=u0, mesh=case["mesh"], dt=case["dt"],
+                                                                     step=case["step"])
+        c = torch.tensor(case["coef"], dtype=torch.float64, requires_grad=True)
+        x = u0.clone().requires_grad_(True)
+        out = case["build"](M, c).integrate(u_0=x, mesh=case["mesh"], dt=case["dt"], step=case["step"])
+        loss = ((out - target) ** 2).mean()
+        loss.backward()
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), u0=u0.numpy(), target=target.numpy(),
+                            loss=np.array(loss.item()), grad_u0=x.grad.numpy(), grad_coef=np.array(c.grad.item()))
+        print(name, "loss", loss.item(), "grad_coef", c.grad.item())
+
     if only:
         return
     # Coefficient tables (integrator/_stable_etdrk/_uncached.py:180-211, _etdrk.py:54-82).

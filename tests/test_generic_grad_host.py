@@ -1,0 +1,58 @@
+"""Gradients of programs outside the hand-written Convection adjoint (vorticity NS, the high-dimensional
+KS with its batch-wide mean, KdV with its complex symbol): d loss / d u0 and d loss / d coef against the
+reference's float64 autograd (golden vectors), on the CPU. The forward steps through the callback path
+with the CPU stand-ins of ``tests/cpu_library.py``; the backward recomputes the segments in torch
+arithmetic and differentiates them with autograd (``adjoint._RecomputeFn``)."""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import cases as C
+import cpu_library as CL
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("name", sorted(C.GENERIC_GRAD_CASES))
+def test_gradients_match_reference_autograd(monkeypatch, name):
+    CL.force_callback(monkeypatch)
+    case = C.GENERIC_GRAD_CASES[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    M = C.namespace("torchfsm_gb300")
+    coef = torch.tensor(case["coef"], dtype=torch.float32, requires_grad=True)
+    op = case["build"](M, coef)
+    u0 = torch.tensor(g["u0"], dtype=torch.float32, requires_grad=True)
+    target = torch.tensor(g["target"], dtype=torch.float32)
+    out = op.integrate(u_0=u0, mesh=case["mesh"], dt=case["dt"], step=case["step"])
+    loss = ((out - target) ** 2).mean()
+    loss.backward()
+    assert abs(loss.item() - float(g["loss"])) <= 1e-4 * abs(float(g["loss"]))
+    ref_u = g["grad_u0"]
+    err_u = float(np.linalg.norm(u0.grad.numpy() - ref_u) / np.linalg.norm(ref_u))
+    err_c = abs(coef.grad.item() - float(g["grad_coef"])) / abs(float(g["grad_coef"]))
+    print(f"{name}: grad u0 rel-L2 {err_u:.2e}, grad coef rel {err_c:.2e}")
+    assert err_u <= 1e-4 and err_c <= 1e-4
+
+
+def test_two_segments_equal_one(monkeypatch):
+    """Checkpoints every 7 steps (three segments) give the gradients of one 20-step segment."""
+    from torchfsm_gb300 import adjoint
+
+    CL.force_callback(monkeypatch)
+    case = C.GENERIC_GRAD_CASES["grad_ns2d_n32"]
+    M = C.namespace("torchfsm_gb300")
+    res = []
+    for K in (50, 7):
+        coef = torch.tensor(case["coef"], dtype=torch.float32, requires_grad=True)
+        op = case["build"](M, coef)
+        u0 = torch.tensor(C.generic_grad_initial_condition("grad_ns2d_n32"), dtype=torch.float32, requires_grad=True)
+        op.integrate(u_0=u0.detach(), mesh=case["mesh"], dt=case["dt"], step=1)
+        with torch.enable_grad():
+            out = adjoint._prepare_and_apply(op, u0, case["dt"], case["step"], K)
+        (out ** 2).mean().backward()
+        res.append((u0.grad.clone(), coef.grad.item()))
+    assert torch.allclose(res[0][0], res[1][0], rtol=1e-5, atol=1e-9)
+    assert abs(res[0][1] - res[1][1]) <= 1e-5 * abs(res[0][1])

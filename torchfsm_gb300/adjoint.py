@@ -300,11 +300,146 @@ class _IntegrateFn(torch.autograd.Function):
         return (grad_u0, None, None, None, None, *grads)
 
 
+def _contour_tables_complex(L: torch.Tensor, dt: float, M: int, r: float):
+    """E, E2 (complex) and c1, c4, c5, c6 (their real parts, as the reference keeps them) of SETDRK4
+    for a complex128 symbol L, in torch arithmetic that autograd differentiates with respect to L
+    (integrator/_stable_etdrk/_uncached.py:8-43, 180-211)."""
+    j = torch.arange(1, M + 1, device=L.device, dtype=torch.float64)
+    roots = torch.exp(2j * math.pi * (j - 0.5) / M)
+    z = r * roots + (L * dt).unsqueeze(-1)
+    ez = torch.exp(z)
+    E = torch.exp(dt * L)
+    E2 = torch.exp(0.5 * dt * L)
+    c1 = dt * ((torch.exp(z / 2) - 1) / z).mean(-1).real
+    c4 = dt * ((-4 - z + ez * (4 - 3 * z + z ** 2)) / z ** 3).mean(-1).real
+    c5 = dt * ((2 + z + ez * (-2 + z)) / z ** 3).mean(-1).real
+    c6 = dt * ((-4 - 3 * z - z ** 2 + ez * (4 - z)) / z ** 3).mean(-1).real
+    return E, E2, c1, c4, c5, c6
+
+
+def _setdrk4_step(u: torch.Tensor, tabs, nonlinear) -> torch.Tensor:
+    """One SETDRK4 step on full spectra in torch arithmetic (integrator/_stable_etdrk/_setdrk_step.py:55-82)."""
+    E, E2, c1, c4, c5, c6 = tabs
+    n0 = nonlinear(u)
+    a1 = E2 * u + c1 * n0
+    n1 = nonlinear(a1)
+    a2 = E2 * u + c1 * n1
+    n2 = nonlinear(a2)
+    a3 = E2 * a1 + c1 * (2 * n2 - n0)
+    n3 = nonlinear(a3)
+    return E * u + c4 * n0 + c5 * 2 * (n1 + n2) + c6 * n3
+
+
+class _RecomputeFn(torch.autograd.Function):
+    """Gradients of a SETDRK4 integration of any program (vorticity, KS, Leray, sources, complex
+    symbols, Python-callable terms): the forward runs the library's integration with checkpoints
+    every ``checkpoint`` steps; the backward recomputes each segment from its checkpoint with the
+    same step written in torch arithmetic on full spectra (the operator's own nonlinear closure, the
+    SETDRK4 tables from the FP64 contour formulas of the operator's linear symbol, rounded to FP32)
+    and differentiates that segment with torch autograd, last segment first. Only one segment's
+    graph is alive at a time."""
+
+    @staticmethod
+    def forward(ctx, u0, op, plan, spectral, dt, steps, checkpoint, *coefs):
+        state = spectral.to_half(u0.detach()).contiguous()
+        checkpoints = [state.clone()]
+        done = 0
+        while done < steps:
+            k = min(checkpoint, steps - done)
+            plan.integrate_half(state, k)
+            done += k
+            if done < steps:
+                checkpoints.append(state.clone())
+        ctx.op, ctx.spectral, ctx.dt, ctx.steps, ctx.checkpoint = op, spectral, dt, steps, checkpoint
+        ctx.checkpoints = checkpoints
+        ctx.save_for_backward(u0, *coefs)
+        return spectral.to_physical(state, keep_input=False)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        op, sp = ctx.op, ctx.spectral
+        u0, *coefs = ctx.saved_tensors
+        steps, K, dt = ctx.steps, ctx.checkpoint, ctx.dt
+        f_mesh = op._state_dict["f_mesh"]
+        C = op._state_dict["n_channel"]
+        nd = len(f_mesh.mesh_info)
+        dims = tuple(range(-nd, 0))
+        from .mesh import FourierMesh
+
+        fm64 = FourierMesh(f_mesh.mesh_info, device=u0.device, dtype=torch.float64)
+        cfg = getattr(op, "_integrator_config", {}) or {}
+        M = int(cfg.get("n_integration_points", 16))
+        r = float(cfg.get("integration_radius", 1.0))
+        nonlinear = op._state_dict["nonlinear_func"]
+        with torch.enable_grad():
+            leaves = [c.detach().requires_grad_(ctx.needs_input_grad[7 + i]) for i, c in enumerate(coefs)]
+            by_id = {id(c): leaf for c, leaf in zip(coefs, leaves)}
+            L = None
+            for coef, core in op._linear_terms:
+                if isinstance(coef, torch.Tensor):
+                    c64 = by_id.get(id(coef), coef.detach()).to(device=u0.device, dtype=torch.float64)
+                else:
+                    c64 = coef
+                term = c64 * core(fm64, C)
+                L = term if L is None else L + term
+            if L is None:
+                L = torch.zeros((1, 1) + (1,) * nd, dtype=torch.complex128, device=u0.device)
+            tabs = [t.to(torch.complex64) if t.is_complex() else t.to(torch.float32)
+                    for t in _contour_tables_complex(L.to(torch.complex128), dt, M, r)]
+            v = grad_out.to(torch.float32)
+            coef_grads = [None] * len(coefs)
+            starts = list(range(0, steps, K))
+            u0_grad = None
+            for si in reversed(range(len(starts))):
+                n = min(K, steps - starts[si])
+                if si == 0:
+                    x_in = u0.detach().to(torch.float32).requires_grad_(ctx.needs_input_grad[0])
+                    y = torch.fft.fftn(x_in, dim=dims).to(torch.complex64)
+                else:
+                    x_in = sp.half_to_full(ctx.checkpoints[si]).to(torch.complex64).detach().requires_grad_(True)
+                    y = x_in
+                for _ in range(n):
+                    y = _setdrk4_step(y, tabs, nonlinear)
+                out = torch.fft.ifftn(y, dim=dims).real if si == len(starts) - 1 else y
+                wanted = [x_in] + [leaf for leaf in leaves if leaf.requires_grad]
+                grads = torch.autograd.grad(out, wanted, grad_outputs=v, allow_unused=True,
+                                            retain_graph=si > 0)
+                j = 1
+                for i, leaf in enumerate(leaves):
+                    if leaf.requires_grad:
+                        g = grads[j]
+                        j += 1
+                        if g is not None:
+                            coef_grads[i] = g if coef_grads[i] is None else coef_grads[i] + g
+                if si == 0:
+                    u0_grad = grads[0]
+                else:
+                    v = grads[0].detach()
+        grads_out = [u0_grad.to(u0.dtype) if (u0_grad is not None and ctx.needs_input_grad[0]) else None]
+        grads_out += [None] * 6
+        for i, c in enumerate(coefs):
+            g = coef_grads[i]
+            grads_out.append(g.to(c.dtype).reshape(c.shape) if g is not None else None)
+        return tuple(grads_out)
+
+
 def integrate_with_grad(op, u0: torch.Tensor, dt: float, steps: int, checkpoint: int = 50) -> torch.Tensor:
     """``op.integrate(u_0=u0, dt=dt, step=steps)`` with gradients to u0 and to tensor coefficients
     of the operator's linear terms (the operator's mesh must be registered)."""
     with torch.no_grad():
         return _prepare_and_apply(op, u0, dt, steps, checkpoint)
+
+
+def _convection_adjoint_applies(op, plan) -> bool:
+    """The hand-written adjoint's programs: fused Convection (C == ndim) without sources, with a real
+    linear symbol."""
+    if not isinstance(plan, _native.NativePlan):
+        return False
+    prog = plan.program
+    if prog.nonlinear != _lib.FSM_NL_CONVECTION or prog.sources:
+        return False
+    L64 = op._linear_coef64(plan.device)
+    return not (L64.is_complex() and float(L64.imag.abs().max()) > 0)
 
 
 def _prepare_and_apply(op, u0, dt, steps, checkpoint):
@@ -313,12 +448,14 @@ def _prepare_and_apply(op, u0, dt, steps, checkpoint):
         op._build_integrator(dt, u0.device)
         integ = op._state_dict["integrator"]
     plan = integ.plan
-    if not isinstance(plan, _native.NativePlan):
-        raise NotImplementedError("gradients are provided for programs the fused kernels run "
-                                  "(not for nonlinear terms stepped through Python callables)")
-    prog = plan.program
-    if plan.integrator != _lib.FSM_SETDRK4:
+    if int(plan.integrator) != _lib.FSM_SETDRK4:
         raise NotImplementedError("gradients are provided for the SETDRK4 integrator")
+    coefs = [c for c, _ in op._linear_terms if isinstance(c, torch.Tensor) and c.requires_grad]
+    if not _convection_adjoint_applies(op, plan):
+        # any other program: segments recomputed and differentiated with torch autograd
+        with torch.enable_grad():
+            return _RecomputeFn.apply(u0, op, plan, integ.spectral, float(dt), int(steps), int(checkpoint), *coefs)
+    prog = plan.program
     L64 = op._linear_coef64(u0.device)
     h = plan.shape[-1] // 2 + 1
     nd = len(plan.shape)

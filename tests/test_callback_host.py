@@ -71,12 +71,27 @@ def test_runge_kutta_with_a_python_callable_is_unsupported(cpu_library):
         op.integrate(u_0=torch.rand(1, 1, 64), mesh=[(0, 1, 64)], dt=0.01, step=2)
 
 
-def test_gradients_of_a_callback_program_are_not_provided(cpu_library):
+def test_gradients_of_a_callback_program_match_central_differences(cpu_library):
+    """A program with a Python-callable term: its gradient (segments recomputed in torch arithmetic
+    and differentiated by autograd) against central differences of the same integration."""
     M = C.namespace("torchfsm_gb300")
     op = 0.05 * M.operator.Laplacian() + M.operator.ImplicitSource(lambda u: u - u ** 3)
-    u0 = torch.rand(1, 1, 64, requires_grad=True)
-    with pytest.raises(NotImplementedError, match="Python callables"):
-        op.integrate(u_0=u0, mesh=[(0, 1, 64)], dt=0.01, step=2)
+    mesh = [(0, 1, 64)]
+    u0 = torch.tensor(C.initial_condition("allencahn1d_n64")[:1], dtype=torch.float32)
+    target = torch.zeros_like(u0)
+
+    def loss_of(u):
+        return ((op.integrate(u_0=u, mesh=mesh, dt=0.01, step=12) - target) ** 2).mean()
+
+    x = u0.clone().requires_grad_(True)
+    loss_of(x).backward()
+    v = torch.tensor(np.random.default_rng(3).standard_normal(u0.shape), dtype=torch.float32)
+    v /= v.norm()
+    eps = 1e-2
+    with torch.no_grad():
+        fd = (loss_of(u0 + eps * v) - loss_of(u0 - eps * v)).item() / (2 * eps)
+    ad = float((x.grad * v).sum())
+    assert abs(fd - ad) <= 2e-2 * abs(ad), (fd, ad)
 
 
 def test_linear_part_that_changes_channels_stays_unsupported(cpu_library):

@@ -440,6 +440,12 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* prog, double 
     for (int j = pre; j < p->h; ++j) prefix = prefix && !keep[p->koff[1] + j];
     if (reg && prefix && pre == n1 / 3 + 1) p->hk = pre;
   }
+  p->wp = p->S / mesh->n[0];
+  if (path == 2) {
+    const int n0 = mesh->n[0], n1 = mesh->n[1];
+    if (is_pow2(n0) && n0 >= 16 && n0 <= 256 && is_pow2(n1) && n1 >= 16 && n1 <= 256) p->wp = (p->h + 1) & ~1;
+  }
+  p->ms = (int64_t)mesh->n[0] * p->wp;
   std::vector<float2> tw(kTwiddleMax);
   for (int k = 0; k < kTwiddleMax; ++k) {
     const double ang = 2.0 * M_PI * (double)k / (double)kTwiddleMax;
@@ -549,7 +555,8 @@ static size_t workspace_layout(const FsmPlan* p, int32_t batch, int32_t steps, s
   bytes += dc;
   if (off_arrays) *off_arrays = bytes;
   if (p->path == 2 || p->path == 4) {
-    const size_t per = (size_t)(p->n_aux * p->C + p->n_mid + p->n_mid2 + p->n_prod) * p->S * sizeof(float2);
+    const size_t per = ((size_t)(p->n_aux * p->C + p->n_mid2) * p->S + (size_t)(p->n_mid + p->n_prod) * p->ms) *
+                       sizeof(float2);
     bytes += align256(per * (size_t)batch);
   }
   return bytes;
@@ -723,14 +730,14 @@ struct SplitEvents {
 // slice of the workspace (the workspace holds the arrays of all samples, sample-major slices).
 StepArgs batch_arrays(const FsmPlan* p, StepArgs a, float2* arr, int b0, int n) {
   const int64_t S = p->S;
-  const int64_t per_sample = (int64_t)(p->n_aux * p->C + p->n_mid + p->n_mid2 + p->n_prod) * S;
+  const int64_t per_sample = (int64_t)(p->n_aux * p->C + p->n_mid2) * S + (int64_t)(p->n_mid + p->n_prod) * p->ms;
   a.state += (int64_t)b0 * p->C * S;
   if (a.traj) a.traj += (int64_t)b0 * a.n_frames * p->C * S;
   if (p->lin_batch > 1) a.tab += (int64_t)b0 * p->lin_ch * S;
   if (a.src && p->src_batch > 1) a.src += (int64_t)b0 * p->C * S;
   a.aux = arr + (int64_t)b0 * per_sample;
   a.mid = a.aux + (int64_t)n * p->n_aux * p->C * S;
-  a.mid2 = a.mid + (int64_t)n * p->n_mid * S;
+  a.mid2 = a.mid + (int64_t)n * p->n_mid * p->ms;
   a.prod = a.mid2 + (int64_t)n * p->n_mid2 * S;
   a.B = n;
   return a;
@@ -834,6 +841,8 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
   a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
   a.tile_zero = p->tile_zero;
   a.hk = p->hk;
+  a.wp = p->wp;
+  a.ms = p->ms;
   a.nm = p->ndim == 3 ? p->n[1] : 1;
   a.tw = p->tw;
   a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));

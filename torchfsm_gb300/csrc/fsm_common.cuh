@@ -338,6 +338,10 @@ struct FsmPlan {
   // register passes run both axes: the fields beyond it are zero, so the column pass does not
   // store them and the row pass does not load them.
   int hk = 0;
+  // Row pitch (complex entries) and field stride of the stage fields and products (workspace
+  // arrays exchanged between the passes). 2D register passes: n1/2 + 1 rounded up to even, so that
+  // rows start on 16-byte boundaries (tensor-map strides); otherwise the unpadded S / n0 and S.
+  int64_t wp = 0, ms = 0;
 };
 
 namespace fsm {

@@ -44,6 +44,7 @@ struct StepArgs {
   int H;
   const uint8_t* tile_zero;  // register axis-0 pass: column tiles whose next-stage fields are zero
   int hk;                     // 2D: last-axis columns of the stage fields stored and read (FsmPlan::hk)
+  int64_t wp, ms;             // row pitch and field stride of mid / prod (FsmPlan::wp, ms)
 };
 
 int transform_r2c_last(int n, const float* in, float2* out, int64_t rows, const float2* tw, cudaStream_t st);

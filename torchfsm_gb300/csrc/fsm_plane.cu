@@ -273,10 +273,9 @@ __global__ void __launch_bounds__(256) k_plane_row(StepArgs a) {
 __global__ void k_ks_mean(StepArgs a, int nx) {
   float acc = 0.f;
   const int total = a.B * nx;
-  const int64_t stride = a.S / nx;
   for (int i = threadIdx.x; i < total; i += blockDim.x) {
     const int b = i / nx, x = i % nx;
-    acc += a.prod[((int64_t)b * a.n_prod) * a.S + (int64_t)x * stride].x;
+    acc += a.prod[((int64_t)b * a.n_prod) * a.ms + (int64_t)x * a.wp].x;
   }
   __shared__ float red[256];
   red[threadIdx.x] = acc;

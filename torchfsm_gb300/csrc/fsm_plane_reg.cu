@@ -296,14 +296,14 @@ __device__ __forceinline__ void axis0_body(const StepArgs& a) {
   for (int cg = 0; cg < C / CG; ++cg) {
     if (a.stage >= 0) {
       for (int f = 0; f < CG; ++f) {
-        const float2* src = a.prod + ((int64_t)b * a.n_prod + cg * CG + f) * S;
+        const float2* src = a.prod + ((int64_t)b * a.n_prod + cg * CG + f) * a.ms;
         // all loads of the tile are issued before the shared-memory stores
         float2 buf[NX * W / 256];
 #pragma unroll
         for (int it = 0; it < NX * W / 256; ++it) {
           const int idx = threadIdx.x + it * 256;
           const int row = idx / W, col = idx % W;
-          if (c0 + col < inner) buf[it] = src[(int64_t)row * inner + c0 + col];
+          if (c0 + col < inner) buf[it] = src[(int64_t)row * a.wp + c0 + col];
         }
 #pragma unroll
         for (int it = 0; it < NX * W / 256; ++it) {
@@ -352,12 +352,12 @@ __device__ __forceinline__ void axis0_body(const StepArgs& a) {
       const int m0 = (KIND == FSM_NL_CONVECTION) ? cg * 2 : 0;
 #pragma unroll 1
       for (int mf = 0; mf < NMO; ++mf) {
-        float2* dst = a.mid + ((int64_t)b * a.n_mid + m0 + mf) * S;
+        float2* dst = a.mid + ((int64_t)b * a.n_mid + m0 + mf) * a.ms;
 #pragma unroll
         for (int it = 0; it < NX * W / 256; ++it) {
           const int idx = threadIdx.x + it * 256;
           const int row = idx / W, cc = idx % W;
-          if (c0 + cc < inner) dst[(int64_t)row * inner + c0 + cc] = make_float2(0.f, 0.f);
+          if (c0 + cc < inner) dst[(int64_t)row * a.wp + c0 + cc] = make_float2(0.f, 0.f);
         }
       }
       continue;  // uniform across the CTA
@@ -397,12 +397,12 @@ __device__ __forceinline__ void axis0_body(const StepArgs& a) {
       for (int j = 0; j < E; ++j) ob[t + T * j] = v[j];
       __syncthreads();
       const int mout = (KIND == FSM_NL_CONVECTION) ? cg * 2 + mf : mf;
-      float2* dst = a.mid + ((int64_t)b * a.n_mid + mout) * S;
+      float2* dst = a.mid + ((int64_t)b * a.n_mid + mout) * a.ms;
 #pragma unroll
       for (int it = 0; it < NX * W / 256; ++it) {
         const int idx = threadIdx.x + it * 256;
         const int row = idx / W, cc = idx % W;
-        if (c0 + cc < ((DIM == 2) ? (int64_t)a.hk : inner)) dst[(int64_t)row * inner + c0 + cc] = tileB[cc * P + row];
+        if (c0 + cc < ((DIM == 2) ? (int64_t)a.hk : inner)) dst[(int64_t)row * a.wp + c0 + cc] = tileB[cc * P + row];
       }
       __syncthreads();
     }
@@ -492,7 +492,8 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
   __syncthreads();
   const int b = blockIdx.y;
   const int r0 = (blockIdx.x * groups + g) * 2;
-  const int64_t S = a.S;
+  const int64_t S = a.ms;  // field stride of the stage fields and products
+  const int64_t WP = a.wp;  // their row pitch
   const float* ky = a.ky;
   const float2* mid = a.mid + (int64_t)b * a.n_mid * S;
   float2* prod = a.prod + (int64_t)b * a.n_prod * S;
@@ -502,7 +503,7 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
     float p[2][E];
 #pragma unroll
     for (int rr = 0; rr < 2; ++rr) {
-      const int64_t roff = (int64_t)(r0 + rr) * H;
+      const int64_t roff = (int64_t)(r0 + rr) * WP;
       float2 Z1[E], Z2[E];
 #pragma unroll
       for (int j = 0; j < E; ++j) {
@@ -542,12 +543,12 @@ __global__ void __launch_bounds__(256, 2) k_plane_row_r(StepArgs a) {
 #pragma unroll
     for (int j = 0; j < E; ++j) zp[j] = make_float2(p[0][j], p[1][j]);
     reg_fft<NY, false>(zp, scr, twt, t);
-    split_store_r<NY>(zp, t, lane, prod + (int64_t)r0 * H, prod + (int64_t)(r0 + 1) * H);
+    split_store_r<NY>(zp, t, lane, prod + (int64_t)r0 * WP, prod + (int64_t)(r0 + 1) * WP);
   } else {
     // convection, C = 2: conv_c = u0 dx u_c + u1 dy u_c
 #pragma unroll 1
     for (int rr = 0; rr < 2; ++rr) {
-      const int64_t roff = (int64_t)(r0 + rr) * H;
+      const int64_t roff = (int64_t)(r0 + rr) * WP;
       float2 Z1[E], Z2[E];
 #pragma unroll
       for (int j = 0; j < E; ++j) {

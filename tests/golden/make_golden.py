@@ -129,9 +129,18 @@ def main(ref_root: str) -> None:
         out = case["build"](M, c).integrate(u_0=x, mesh=case["mesh"], dt=case["dt"], step=case["step"])
         loss = ((out - target) ** 2).mean()
         loss.backward()
+        # the FP32 floor: the reference's own float32 autograd on the same inputs, against its float64
+        # gradient (stiff symbols such as KdV's i k^3 amplify the rounding of every step)
+        c32 = torch.tensor(case["coef"], dtype=torch.float32, requires_grad=True)
+        x32 = u0.float().requires_grad_(True)
+        out32 = case["build"](M, c32).integrate(u_0=x32, mesh=case["mesh"], dt=case["dt"], step=case["step"])
+        ((out32 - target.float()) ** 2).mean().backward()
+        fp32_u = float(torch.linalg.vector_norm(x32.grad.double() - x.grad) / torch.linalg.vector_norm(x.grad))
+        fp32_c = abs(c32.grad.item() - c.grad.item()) / abs(c.grad.item())
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), u0=u0.numpy(), target=target.numpy(),
-                            loss=np.array(loss.item()), grad_u0=x.grad.numpy(), grad_coef=np.array(c.grad.item()))
-        print(name, "loss", loss.item(), "grad_coef", c.grad.item())
+                            loss=np.array(loss.item()), grad_u0=x.grad.numpy(), grad_coef=np.array(c.grad.item()),
+                            fp32_grad_u0_rel_l2=np.array(fp32_u), fp32_grad_coef_rel=np.array(fp32_c))
+        print(name, "loss", loss.item(), "grad_coef", c.grad.item(), "fp32 floor", fp32_u, fp32_c)
 
     if only:
         return

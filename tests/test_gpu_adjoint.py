@@ -154,5 +154,9 @@ def test_recomputed_segments_match_reference_autograd(name):
     ref_u = g["grad_u0"]
     err_u = float(np.linalg.norm(u0.grad.cpu().numpy() - ref_u) / np.linalg.norm(ref_u))
     err_c = abs(coef.grad.item() - float(g["grad_coef"])) / abs(float(g["grad_coef"]))
-    print(f"{name}: grad u0 rel-L2 {err_u:.2e}, grad coef rel {err_c:.2e}")
-    assert err_u <= 1e-4 and err_c <= 1e-4
+    # 1e-4, or twice the reference's own float32 autograd error where that floor is higher (KdV: the
+    # i k^3 symbol amplifies every step's rounding; the reference's FP32 gradient is 1.9e-4 off)
+    tol_u = max(1e-4, 2 * float(g["fp32_grad_u0_rel_l2"]))
+    tol_c = max(1e-4, 2 * float(g["fp32_grad_coef_rel"]))
+    print(f"{name}: grad u0 rel-L2 {err_u:.2e} (bound {tol_u:.1e}), grad coef rel {err_c:.2e} (bound {tol_c:.1e})")
+    assert err_u <= tol_u and err_c <= tol_c

@@ -840,7 +840,16 @@ def run_serving(args):
     device = torch.device("cuda", 0)
     count = args.requests
     reqs = serving.make_stream(count, seed=7, rate_hz=0.0)
-    server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk, priority=args.priority)
+    phase, t_phase = {}, time.perf_counter()
+
+    def mark(name):
+        nonlocal t_phase
+        now = time.perf_counter()
+        phase[name] = now - t_phase
+        t_phase = now
+
+    server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk, priority=args.priority,
+                                 group_lines=bool(args.group_lines))
     server.prepare(sorted({(r.kind, r.n) for r in reqs}))
     # warm-up: a few requests through both paths (kernel attributes, plans of the plain path)
     warm = serving.make_stream(8, seed=99, rate_hz=0.0, max_steps=120)
@@ -850,8 +859,10 @@ def run_serving(args):
         serving.solve_alone(r, device, ops)
     total = sum(r.dof_steps for r in reqs)
     run = server.run_threaded if args.threaded else server.run
+    mark("setup_and_warmup")
     # burst: every request waiting at t = 0
     wall = run(reqs, realtime=False)
+    mark("burst")
     serve_tp = total / wall
     burst_lat = [r.t_done - r.arrival for r in reqs]
     # the plain drop-in, one solve at a time, same requests in the same order
@@ -865,6 +876,7 @@ def run_serving(args):
         ref = res.double()
         max_err = max(max_err, float((r.result.double() - ref).norm() / max(ref.norm(), 1e-30)))
     nonfinite_serve = [r.rid for r in reqs if r.finite is False]
+    mark("plain")
     # the reference's own path on bounded samples of the same stream (cheapest requests first),
     # beside our one-at-a-time path on the same requests
     alone_by_rid = {r.rid: t for r, t in zip(reqs, alone_t)}
@@ -877,6 +889,7 @@ def run_serving(args):
             res["plain_value_same_requests"] = dof / ours_s if ours_s > 0 else None
         reference_sample[leg] = res
     plain_tp = total / sum(alone_t)
+    mark("reference_samples")
     # Poisson arrivals at rates below the server's measured capacity: latency of each request
     # against its own one-at-a-time time (the streams hold the same requests at every rate)
     sweep = []
@@ -892,6 +905,7 @@ def run_serving(args):
                       "p99_over_isolated_p99": _pctl(lt, 99) / _pctl(alone_t, 99)})
         if load == args.load:
             rate, wall2, lat, ratio = load * count / wall, w, lt, rt
+    mark("poisson_sweep")
     line = {"metric": "DOF*steps/s of a mixed solve stream (continuous batching vs one solve at a time)",
             "value": serve_tp, "unit": "DOF*steps/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "ms_per_step": wall * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -909,7 +923,8 @@ def run_serving(args):
                         "latency_s": {"p50": _pctl(lat, 50), "p99": _pctl(lat, 99)},
                         "isolated_latency_s": {"p50": _pctl(alone_t, 50), "p99": _pctl(alone_t, 99)},
                         "latency_over_isolated": {"p50": _pctl(ratio, 50), "p99": _pctl(ratio, 99)},
-                        "poisson_sweep": sweep, "graph_replays": server.graph_replays,
+                        "poisson_sweep": sweep, "graph_replays": server.graph_replays, "phase_seconds": phase,
+                        "line_groups": [[b.n for b in g.buckets] for g in server.groups],
                         "target": "throughput >= 3x the plain path (burst); p99 latency <= 2x the isolated p99 "
                                   "(same requests one at a time) at a stated Poisson load",
                         "loads_meeting_p99_target": [x["load"] for x in sweep if x["p99_over_isolated_p99"] <= 2.0],
@@ -1140,7 +1155,8 @@ def _summary(line: dict, keys) -> dict:
 def other_workloads(args) -> dict:
     """The other named workloads, run after the headline's timed region and summarised on its line:
     1D Burgers N=128 solve latency, 3D Burgers 256^3 throughput with its FP64 error after 50 steps,
-    and the differentiable 2D Burgers forward + backward with its gradient checks. Each runs with few
+    the differentiable 2D Burgers forward + backward with its gradient checks, and the serving
+    stream (burst throughput against the plain path, latency at one Poisson load). Each runs with few
     repetitions (its own workload line, ``--workload``, has the full figures); a failure is reported
     and leaves the headline intact."""
     import argparse as _ap
@@ -1162,6 +1178,16 @@ def other_workloads(args) -> dict:
                                                                      "reference_autograd.rel_l2_grad_u0_vs_adjoint",
                                                                      "reference_autograd.rel_diff_grad_nu_vs_adjoint"]),
     }
+    serve = _ap.Namespace(**dict(vars(args), requests=args.serve_summary_requests, loads=str(args.load),
+                                 ref_requests=0, ref_cpu_requests=0))
+    if args.serve_summary_requests > 0:
+        legs[f"serving_{args.serve_summary_requests}_requests"] = (
+            lambda _a: run_serving(serve),
+            ["value", "unit", "config.workload", "serving.throughput_plain", "serving.speedup_vs_plain",
+             "serving.poisson_rate_hz", "serving.latency_s", "serving.isolated_latency_s",
+             "serving.latency_over_isolated", "serving.poisson_sweep", "serving.loads_meeting_p99_target",
+             "serving.max_rel_diff_mix_vs_alone", "serving.nonfinite_requests", "serving.line_groups",
+             "serving.phase_seconds", "gpu_launches"])
     out = {}
     for name, (fn, keys) in legs.items():
         t0 = time.perf_counter()
@@ -1244,6 +1270,11 @@ def main():
                     help="serving: requests of the stream run by the reference's CPU path")
     ap.add_argument("--load", type=float, default=0.35, help="serving: the Poisson rate whose figures head the line, as a fraction of capacity")
     ap.add_argument("--threaded", type=int, default=1, help="serving: one host worker thread per bucket")
+    ap.add_argument("--serve-summary-requests", type=int, default=2000,
+                    help="ns2d: requests of the serving stream summarised on the headline line after its timed "
+                         "region (burst, plain path, one Poisson load; 0: skip)")
+    ap.add_argument("--group-lines", type=int, default=1,
+                    help="serving: the 1D KS buckets of every size advance together, one launch per tick")
     ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],
                     help="serving: buckets on the high-priority streams")
     ap.add_argument("--workload", default="ns2d",

@@ -296,6 +296,34 @@ int fsm_serve_request_status(FsmServe* server, int64_t request_id, int32_t* stat
 int fsm_serve_stats(FsmServe* server, int64_t* stats, int32_t n);
 int fsm_serve_destroy(FsmServe* server);
 
+/* Serving groups: engines of different grid sizes (and PDEs) ticked together. No counterpart in
+ * the reference (see the serving engine above).
+ *
+ * fsm_serve_group_create: 1 to 8 engines that share one stream and have no tick in flight. From
+ *   then on they are ticked only through the group (fsm_serve_tick on a member is refused);
+ *   requests are still submitted to, polled from (fsm_serve_poll reports the completed ids),
+ *   cancelled at and queried from the members. tick_ms as in fsm_serve_create, measured per
+ *   step and occupied slot over the whole group.
+ * fsm_serve_group_tick: admit into every member, then advance every occupied slot of every
+ *   member by the same k steps (the fewest remaining steps of any active request, at most the
+ *   smallest member chunk and the tick_ms bound). When every member is a 1D line plan of 256 to
+ *   4096 points and one nonlinear kind (KS or Burgers), the tick is ONE kernel launch over all
+ *   of them; otherwise the members are launched one after the other in the tick (lockstep).
+ *   *steps_launched = k, 0 when a tick is in flight or no slot is occupied.
+ * fsm_serve_group_poll: complete the group's tick once the device has finished it (wait != 0:
+ *   block until then): every member's finished requests leave as in fsm_serve_poll;
+ *   *in_flight = 1 while the tick is still running.
+ * fsm_serve_group_stats: up to n of {ticks, kernel launches, tick in flight, one launch per tick}.
+ * fsm_serve_group_destroy: waits for the stream, accounts a finished tick, releases the members
+ *   (which may then be ticked alone or destroyed; destroying a member of a group is refused). */
+typedef struct FsmServeGroup FsmServeGroup;
+#define FSM_SERVE_GROUP_NSTATS 4
+int fsm_serve_group_create(FsmServe* const* engines, int32_t count, double tick_ms, FsmServeGroup** out);
+int fsm_serve_group_tick(FsmServeGroup* group, int32_t* steps_launched);
+int fsm_serve_group_poll(FsmServeGroup* group, int32_t wait, int32_t* in_flight);
+int fsm_serve_group_stats(FsmServeGroup* group, int64_t* stats, int32_t n);
+int fsm_serve_group_destroy(FsmServeGroup* group);
+
 /* Copy the message of the last failure on this host thread into buf. */
 int fsm_last_error(char* buf, size_t len);
 

@@ -86,6 +86,11 @@ EXPORTS = (
     "fsm_serve_request_status",
     "fsm_serve_stats",
     "fsm_serve_destroy",
+    "fsm_serve_group_create",
+    "fsm_serve_group_tick",
+    "fsm_serve_group_poll",
+    "fsm_serve_group_stats",
+    "fsm_serve_group_destroy",
     "fsm_last_error",
     "fsm_abi_version",
 )
@@ -177,6 +182,11 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_serve_request_status.argtypes = [vp, i64, pi32, pi32]
         lib.fsm_serve_stats.argtypes = [vp, pi64, i32]
         lib.fsm_serve_destroy.argtypes = [vp]
+        lib.fsm_serve_group_create.argtypes = [ctypes.POINTER(vp), i32, ctypes.c_double, ctypes.POINTER(vp)]
+        lib.fsm_serve_group_tick.argtypes = [vp, pi32]
+        lib.fsm_serve_group_poll.argtypes = [vp, i32, pi32]
+        lib.fsm_serve_group_stats.argtypes = [vp, pi64, i32]
+        lib.fsm_serve_group_destroy.argtypes = [vp]
         lib.fsm_last_error.argtypes = [ctypes.c_char_p, sz]
         for name in EXPORTS:
             getattr(lib, name).restype = ctypes.c_int

@@ -382,6 +382,54 @@ class ServePool:
         return dict(zip(self.STATS, list(arr)))
 
 
+class ServeGroup:
+    """Serving engines of different grid sizes ticked together (``fsm_serve_group_*``): one tick
+    advances every occupied slot of every member by the same number of steps, as ONE kernel
+    launch when every member is a 1D line plan of one nonlinear kind, else the members one after
+    the other. The members share one stream; requests are still submitted to and polled from
+    them. Close the group before its members."""
+
+    STATS = ("ticks", "launches", "in_flight", "one_launch")
+
+    def __init__(self, pools: List[ServePool], tick_ms: float = 0.0):
+        self.pools = list(pools)
+        self.handle = None
+        arr = (ctypes.c_void_p * len(self.pools))(*[p.handle.value for p in self.pools])
+        handle = ctypes.c_void_p()
+        _lib.check(_lib.load().fsm_serve_group_create(arr, len(self.pools), float(tick_ms), ctypes.byref(handle)))
+        self.handle = handle
+
+    def close(self) -> None:
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self.handle = None
+            _lib.check(_lib.load().fsm_serve_group_destroy(h))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def tick(self) -> int:
+        """Admit into every member and launch the group's next tick; the steps launched (0: busy or idle)."""
+        k = ctypes.c_int32()
+        _lib.check(_lib.load().fsm_serve_group_tick(self.handle, ctypes.byref(k)))
+        return int(k.value)
+
+    def poll(self, wait: bool = False) -> bool:
+        """Complete the group's tick if it is done (or wait for it); whether a tick is still in flight.
+        The members' completed ids are then read with their ``poll``."""
+        busy = ctypes.c_int32()
+        _lib.check(_lib.load().fsm_serve_group_poll(self.handle, 1 if wait else 0, ctypes.byref(busy)))
+        return bool(busy.value)
+
+    def stats(self) -> dict:
+        arr = (ctypes.c_int64 * len(self.STATS))()
+        _lib.check(_lib.load().fsm_serve_group_stats(self.handle, arr, len(self.STATS)))
+        return dict(zip(self.STATS, list(arr)))
+
+
 def warn_precision(dtype: torch.dtype) -> None:
     global _WARNED_FP64
     if dtype == torch.float64 and not _WARNED_FP64:

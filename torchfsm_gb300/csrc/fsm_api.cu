@@ -782,6 +782,54 @@ struct PlaneSequence {
   }
 };
 
+}  // namespace
+
+namespace fsm {
+// The kernels' arguments for `batch` samples of `state` advanced by `steps` steps, without
+// recording (no trajectory, no record slots, no batch-mean scratch).
+StepArgs base_args(const FsmPlan* p, void* state, int32_t batch, int32_t steps) {
+  StepArgs a;
+  memset(&a, 0, sizeof(a));
+  a.state = (float2*)state;
+  a.slot = -1;
+  a.tab = p->tab;
+  a.ts = p->tstride;
+  a.lin_batch = p->lin_batch;
+  a.lin_ch = p->lin_ch;
+  a.src = p->source;
+  a.src_batch = p->src_batch;
+  a.kx = p->kvec + p->koff[0];
+  a.ky = p->kvec + p->koff[p->ndim - 1];
+  a.km = p->kvec + p->koff[p->ndim == 3 ? 1 : 0];
+  a.keepx = p->keep + p->koff[0];
+  a.keepy = p->keep + p->koff[p->ndim - 1];
+  a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
+  a.tile_zero = p->tile_zero;
+  a.hk = p->hk;
+  a.wp = p->wp;
+  a.ms = p->ms;
+  a.nm = p->ndim == 3 ? p->n[1] : 1;
+  a.tw = p->tw;
+  a.coef = p->nl_coef;
+  a.scale = (float)(1.0 / (double)p->R);
+  a.C = p->C;
+  a.n_aux = p->n_aux;
+  a.n_mid = p->n_mid;
+  a.n_prod = p->n_prod;
+  a.n_mid2 = p->n_mid2;
+  a.integ = p->integ;
+  a.nstages = p->nstages;
+  a.steps = steps;
+  a.B = batch;
+  a.flags = p->flags;
+  a.S = p->S;
+  a.H = p->h;
+  return a;
+}
+}  // namespace fsm
+
+namespace {
+
 int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
                    int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof,
                    bool allow_split = true) {
@@ -820,46 +868,11 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
                                          cudaMemcpyHostToDevice, st), "copy record slots")))
       return rc;
   }
-  StepArgs a;
-  memset(&a, 0, sizeof(a));
-  a.state = (float2*)state;
+  StepArgs a = base_args(p, state, batch, steps);
   a.traj = (float2*)traj;
   a.n_frames = n_frames;
-  a.slot = -1;
   a.slots = record_slot ? d_slots : nullptr;
-  a.tab = p->tab;
-  a.ts = p->tstride;
-  a.lin_batch = p->lin_batch;
-  a.lin_ch = p->lin_ch;
-  a.src = p->source;
-  a.src_batch = p->src_batch;
-  a.kx = p->kvec + p->koff[0];
-  a.ky = p->kvec + p->koff[p->ndim - 1];
-  a.km = p->kvec + p->koff[p->ndim == 3 ? 1 : 0];
-  a.keepx = p->keep + p->koff[0];
-  a.keepy = p->keep + p->koff[p->ndim - 1];
-  a.keepm = p->keep + p->koff[p->ndim == 3 ? 1 : 0];
-  a.tile_zero = p->tile_zero;
-  a.hk = p->hk;
-  a.wp = p->wp;
-  a.ms = p->ms;
-  a.nm = p->ndim == 3 ? p->n[1] : 1;
-  a.tw = p->tw;
   a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));
-  a.coef = p->nl_coef;
-  a.scale = (float)(1.0 / (double)p->R);
-  a.C = p->C;
-  a.n_aux = p->n_aux;
-  a.n_mid = p->n_mid;
-  a.n_prod = p->n_prod;
-  a.n_mid2 = p->n_mid2;
-  a.integ = p->integ;
-  a.nstages = p->nstages;
-  a.steps = steps;
-  a.B = batch;
-  a.flags = p->flags;
-  a.S = p->S;
-  a.H = p->h;
 
   if (p->path == 3) return timed(prof, kProfOther, [&] { return launch_pointwise(p, a, st); });
   if (p->path == 1) return timed(prof, kProfOther, [&] { return launch_line(p, a, st); });

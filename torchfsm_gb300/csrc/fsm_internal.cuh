@@ -47,6 +47,10 @@ struct StepArgs {
   int64_t wp, ms;             // row pitch and field stride of mid / prod (FsmPlan::wp, ms)
 };
 
+// The kernels' arguments for `batch` samples of `state` advanced by `steps` steps of plan p,
+// without recording (fsm_api.cu).
+StepArgs base_args(const FsmPlan* p, void* state, int32_t batch, int32_t steps);
+
 int transform_r2c_last(int n, const float* in, float2* out, int64_t rows, const float2* tw, cudaStream_t st);
 int transform_c2r_last(int n, const float2* in, float* out, int64_t rows, float scale, const float2* tw,
                        cudaStream_t st);
@@ -72,6 +76,19 @@ int launch_volume_axis2(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_volume_axis1_fwd(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
+
+// One launch of the 1D line kernel over the samples of several plans of different lengths
+// (256..4096 points, one nonlinear kind): entry j advances a[j].B samples of a[j] by a[j].steps
+// steps (the same for every entry), without recording. cta0 is filled in by the launcher.
+constexpr int kLineMultiMax = 8;
+constexpr int kLineMultiThreads = 256;
+struct LineMulti {
+  StepArgs a[kLineMultiMax];
+  int32_t n[kLineMultiMax];
+  int32_t cta0[kLineMultiMax + 1];
+  int32_t count;
+};
+int launch_line_multi(LineMulti& m, int kind, cudaStream_t st);
 // Register-FFT plane passes (64..256 points per axis); return -1 when no kernel covers the sizes.
 int launch_plane_col_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_row_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);

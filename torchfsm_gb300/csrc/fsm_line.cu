@@ -44,30 +44,29 @@ __device__ __forceinline__ void line_build(float2* __restrict__ Z, int k, float2
   }
 }
 
+// One sample's integration by G = LineCfg<N>::G threads (t < G): the twiddles `tw` are in shared
+// memory already (visible after the body's first barrier); Z (N), u, acc, q (running sums, n_aux
+// arrays H apart) are the sample's shared-memory region. Every thread of the CTA runs the body the
+// same number of times (its barriers are CTA-wide); `active` false runs it on the data of a valid
+// sample without writing global memory (spare sub-groups of a k_line_multi CTA).
 template <int N, int KIND>
-__global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
+__device__ __forceinline__ void line_body(const StepArgs& a, int b, int t, const float2* __restrict__ tw,
+                                          float2* __restrict__ Z, float2* __restrict__ u, bool active) {
   using Cfg = LineCfg<N>;
   constexpr int H = Cfg::H;
   constexpr int G = Cfg::G;
-  extern __shared__ float2 smem[];
-  float2* tw = smem;
-  float2* Z = tw + N;
-  float2* u = Z + N;
   float2* acc = u + H;  // running sums: acc, q (Runge-Kutta: n_aux arrays H apart)
   float2* q = acc + H;
-  const int b = blockIdx.x;
-  const int t = threadIdx.x;
-  load_twiddles(tw, a.tw, kTwiddleMax, N, t, G);
   float2* gstate = a.state + (int64_t)b * H;
   for (int k = t; k < H; k += G) u[k] = gstate[k];
   const int64_t toff = (int64_t)(a.lin_batch > 1 ? b : 0) * H;
   const float2* tab = a.tab + toff;
   const float2* src = a.src ? a.src + (int64_t)(a.src_batch > 1 ? b : 0) * H : nullptr;
   const int slot0 = a.slots ? a.slots[0] : -1;
-  if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && t == 0)
-    a.dc[(int64_t)a.steps * a.nstages * a.B + b] = u[0];  // initial k = 0 value
+  const bool dc = KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && active;
+  if (dc && t == 0) a.dc[(int64_t)a.steps * a.nstages * a.B + b] = u[0];  // initial k = 0 value
   for (int k = t; k < H; k += G) {
-    if (slot0 >= 0) a.traj[((int64_t)b * a.n_frames + slot0) * H + k] = u[k];
+    if (slot0 >= 0 && active) a.traj[((int64_t)b * a.n_frames + slot0) * H + k] = u[k];
     if (a.steps > 0) line_build<N, KIND>(Z, k, u[k], (float)a.keepx[k], a.kx[k], a.scale);
   }
   __syncthreads();
@@ -88,17 +87,71 @@ __global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
       for (int k = t; k < H; k += G) {
         float2 nv = cscale(Z[k], a.coef);
         // k = 0 of the product, for the batch-mean fix-up (k_line_dc_fixup)
-        if (KIND == FSM_NL_KS && (a.flags & FSM_FLAG_REMOVE_MEAN) && k == 0)
-          a.dc[((int64_t)step * ns + s) * a.B + b] = Z[0];
+        if (dc && k == 0) a.dc[((int64_t)step * ns + s) * a.B + b] = Z[0];
         if (src) nv = cadd(nv, src[k]);
         const float2 nxt = etd_stage(a.integ, s, nv, u + k, acc + k, q + k, tab + k, a.ts, H);
         if (!final_stage) line_build<N, KIND>(Z, k, nxt, (float)a.keepx[k], a.kx[k], a.scale);
-        if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H + k] = u[k];
+        if (slot >= 0 && active) a.traj[((int64_t)b * a.n_frames + slot) * H + k] = u[k];
       }
       __syncthreads();
     }
   }
-  for (int k = t; k < H; k += G) gstate[k] = u[k];
+  if (active)
+    for (int k = t; k < H; k += G) gstate[k] = u[k];
+}
+
+template <int N, int KIND>
+__global__ void __launch_bounds__(LineCfg<N>::G) k_line(StepArgs a) {
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  load_twiddles(tw, a.tw, kTwiddleMax, N, threadIdx.x, LineCfg<N>::G);
+  line_body<N, KIND>(a, blockIdx.x, threadIdx.x, tw, tw + N, tw + 2 * N, true);
+}
+
+// Serving: the lines of several plans (one per grid size) advanced by one launch. CTAs
+// [cta0[j], cta0[j + 1]) belong to plan j; each holds kLineMultiThreads / G samples of its plan,
+// one per sub-group of G threads, with the twiddles shared and a region per sample.
+template <int N>
+struct LineMultiCfg {
+  static constexpr int G = LineCfg<N>::G;
+  static constexpr int P = kLineMultiThreads / G;  // samples per CTA
+  static constexpr int H = N / 2 + 1;
+  __host__ __device__ static size_t region(int n_aux) { return (size_t)N + (size_t)(1 + (n_aux > 2 ? n_aux : 2)) * H; }
+  static size_t smem(int n_aux) { return ((size_t)N + P * region(n_aux)) * sizeof(float2); }
+};
+
+template <int N, int KIND>
+__device__ __forceinline__ void line_multi_cta(const StepArgs& a, int cta) {
+  using Cfg = LineMultiCfg<N>;
+  extern __shared__ float2 smem[];
+  float2* tw = smem;
+  load_twiddles(tw, a.tw, kTwiddleMax, N, threadIdx.x, kLineMultiThreads);
+  const int sub = threadIdx.x / Cfg::G, t = threadIdx.x % Cfg::G;
+  const int b = cta * Cfg::P + sub;
+  const bool active = b < a.B;
+  float2* Z = smem + N + (size_t)sub * Cfg::region(a.n_aux);
+  line_body<N, KIND>(a, active ? b : a.B - 1, t, tw, Z, Z + N, active);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kLineMultiThreads) k_line_multi(const __grid_constant__ LineMulti m) {
+  int j = 0;
+  while (j + 1 < m.count && (int)blockIdx.x >= m.cta0[j + 1]) ++j;
+  const int cta = (int)blockIdx.x - m.cta0[j];
+  switch (m.n[j]) {
+    case 256: line_multi_cta<256, KIND>(m.a[j], cta); break;
+    case 512: line_multi_cta<512, KIND>(m.a[j], cta); break;
+    case 1024: line_multi_cta<1024, KIND>(m.a[j], cta); break;
+    case 2048: line_multi_cta<2048, KIND>(m.a[j], cta); break;
+    case 4096: line_multi_cta<4096, KIND>(m.a[j], cta); break;
+  }
+}
+
+template <int N>
+static void line_multi_shape(int n_aux, int batch, size_t* smem, int* ctas) {
+  using Cfg = LineMultiCfg<N>;
+  *smem = Cfg::smem(n_aux);
+  *ctas = (batch + Cfg::P - 1) / Cfg::P;
 }
 
 template <int N, int KIND>
@@ -173,6 +226,41 @@ __global__ void k_line_dc_fixup(StepArgs a) {
     if (slot >= 0) a.traj[((int64_t)b * a.n_frames + slot) * H] = u;
   }
   a.state[(int64_t)b * H] = u;
+}
+
+int launch_line_multi(LineMulti& m, int kind, cudaStream_t st) {
+  if (m.count < 1 || m.count > kLineMultiMax) return set_error(FSM_ERR_INVALID, "line multi: plan count");
+  size_t smem = 0;
+  int total = 0;
+  for (int j = 0; j < m.count; ++j) {
+    size_t sm = 0;
+    int ctas = 0;
+    const int B = m.a[j].B, na = m.a[j].n_aux;
+    if (B < 1) return set_error(FSM_ERR_INVALID, "line multi: empty plan entry");
+    switch (m.n[j]) {
+      case 256: line_multi_shape<256>(na, B, &sm, &ctas); break;
+      case 512: line_multi_shape<512>(na, B, &sm, &ctas); break;
+      case 1024: line_multi_shape<1024>(na, B, &sm, &ctas); break;
+      case 2048: line_multi_shape<2048>(na, B, &sm, &ctas); break;
+      case 4096: line_multi_shape<4096>(na, B, &sm, &ctas); break;
+      default: return set_error(FSM_ERR_UNSUPPORTED, "line multi: lengths 256..4096 only");
+    }
+    m.cta0[j] = total;
+    total += ctas;
+    smem = sm > smem ? sm : smem;
+  }
+  m.cta0[m.count] = total;
+  int rc;
+  if (kind == FSM_NL_KS) {
+    if ((rc = prep_smem(k_line_multi<FSM_NL_KS>, smem))) return rc;
+    k_line_multi<FSM_NL_KS><<<total, kLineMultiThreads, smem, st>>>(m);
+  } else if (kind == FSM_NL_CONVECTION) {
+    if ((rc = prep_smem(k_line_multi<FSM_NL_CONVECTION>, smem))) return rc;
+    k_line_multi<FSM_NL_CONVECTION><<<total, kLineMultiThreads, smem, st>>>(m);
+  } else {
+    return set_error(FSM_ERR_UNSUPPORTED, "line multi: unsupported nonlinear term");
+  }
+  return cuda_check(cudaGetLastError(), "k_line_multi");
 }
 
 int launch_line(const FsmPlan* p, const StepArgs& a, cudaStream_t st) {

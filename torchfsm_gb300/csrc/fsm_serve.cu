@@ -52,6 +52,7 @@ struct FsmServe {
   std::unordered_map<uint64_t, std::list<std::pair<uint64_t, cudaGraphExec_t>>::iterator> graphs;
   std::unordered_set<uint64_t> seen;
   std::vector<int64_t> done_ids;  // completed, not yet reported
+  FsmServeGroup* group = nullptr;  // ticked by this group (fsm_serve_group_*), not on its own
   int64_t launches = 0, replays = 0, ticks = 0, slot_steps = 0, completed = 0, cancelled = 0;
   std::mutex mu;
 
@@ -149,22 +150,15 @@ int advance(FsmServe* s, int32_t n, int32_t k, int64_t* launches) {
   return fsm_plan_launch_count(s->plan, n, k, launches);
 }
 
-// Complete the tick in flight if the device has finished it (or, with wait, once it has).
-int finish_tick(FsmServe* s, bool wait) {
-  if (!s->in_flight) return FSM_OK;
-  cudaError_t q = wait ? cudaEventSynchronize(s->e1) : cudaEventQuery(s->e1);
-  if (q == cudaErrorNotReady) return FSM_OK;
-  int rc;
-  if ((rc = cuda_check(q, "serve tick query"))) return rc;
-  float ms = 0.f;
-  if ((rc = cuda_check(cudaEventElapsedTime(&ms, s->e0, s->e1), "serve tick time"))) return rc;
-  const double per = (double)ms / ((double)s->tick_k * s->tick_n);
-  s->step_ms = s->step_ms > 0.0 ? 0.5 * (s->step_ms + per) : per;
+// Account a completed tick of k steps: finished requests write their outputs and leave, cancelled
+// ones leave, the remaining slots are compacted.
+int complete_tick(FsmServe* s) {
   s->in_flight = false;
   std::vector<fsm::ServeRequest*> fin = s->pool.advance(s->tick_k);
   std::vector<fsm::ServeRequest*> cancels = s->pool.pending_cancels();
   std::vector<fsm::ServeRequest*> leaving = fin;
   leaving.insert(leaving.end(), cancels.begin(), cancels.end());
+  int rc;
   if ((rc = retire(s, leaving))) return rc;
   for (fsm::ServeRequest* r : fin) {
     r->status = fsm::kServeDone;
@@ -176,6 +170,43 @@ int finish_tick(FsmServe* s, bool wait) {
     s->pool.erase(r->id);
   }
   return FSM_OK;
+}
+
+// Complete the tick in flight if the device has finished it (or, with wait, once it has).
+// An engine of a group completes its ticks through fsm_serve_group_poll.
+int finish_tick(FsmServe* s, bool wait) {
+  if (!s->in_flight || s->group) return FSM_OK;
+  cudaError_t q = wait ? cudaEventSynchronize(s->e1) : cudaEventQuery(s->e1);
+  if (q == cudaErrorNotReady) return FSM_OK;
+  int rc;
+  if ((rc = cuda_check(q, "serve tick query"))) return rc;
+  float ms = 0.f;
+  if ((rc = cuda_check(cudaEventElapsedTime(&ms, s->e0, s->e1), "serve tick time"))) return rc;
+  const double per = (double)ms / ((double)s->tick_k * s->tick_n);
+  s->step_ms = s->step_ms > 0.0 ? 0.5 * (s->step_ms + per) : per;
+  return complete_tick(s);
+}
+
+// Admit the waiting requests that fit: their spectra copied into their slots, their slots'
+// coefficient tables recomputed for their dt.
+int admit(FsmServe* s) {
+  int rc;
+  for (const fsm::ServeRequest* r : s->pool.admit()) {
+    const int32_t slot0 = r->slots.front();
+    if ((rc = copy_slots(s, slot0, r->batch, const_cast<void*>(r->u0), true))) return rc;
+    if ((rc = fsm::set_batch_dt_range(s->plan, slot0, r->batch, r->dt, s->st))) return rc;
+  }
+  return FSM_OK;
+}
+
+// Round a graph-replayed tick's step count down to a power of two.
+int32_t graph_steps(int32_t flags, int32_t k) {
+  if ((flags & FSM_SERVE_GRAPHS) && k <= kGraphMaxSteps) {
+    int32_t p2 = 1;
+    while (p2 * 2 <= k) p2 *= 2;
+    return p2;
+  }
+  return k;
 }
 
 }  // namespace
@@ -232,24 +263,16 @@ int fsm_serve_tick(FsmServe* s, int32_t* steps_launched) {
   if (!s) return set_error(FSM_ERR_INVALID, "serve_tick arguments");
   std::lock_guard<std::mutex> g(s->mu);
   if (steps_launched) *steps_launched = 0;
+  if (s->group) return set_error(FSM_ERR_INVALID, "serve_tick: the engine belongs to a group (fsm_serve_group_tick)");
   if (s->in_flight) return FSM_OK;
   int rc;
-  for (const fsm::ServeRequest* r : s->pool.admit()) {
-    const int32_t slot0 = r->slots.front();
-    if ((rc = copy_slots(s, slot0, r->batch, const_cast<void*>(r->u0), true))) return rc;
-    if ((rc = fsm::set_batch_dt_range(s->plan, slot0, r->batch, r->dt, s->st))) return rc;
-  }
+  if ((rc = admit(s))) return rc;
   const int32_t n = s->pool.occupied();
   if (n == 0) return FSM_OK;
   int32_t limit = 0;
   if (s->step_ms > 0.0 && s->tick_ms > 0.0)
     limit = (int32_t)std::max(1.0, std::min(1e9, s->tick_ms / (s->step_ms * n)));
-  int32_t k = s->pool.tick_steps(s->chunk, limit);
-  if ((s->flags & FSM_SERVE_GRAPHS) && k <= kGraphMaxSteps) {
-    int32_t p2 = 1;
-    while (p2 * 2 <= k) p2 *= 2;
-    k = p2;
-  }
+  const int32_t k = graph_steps(s->flags, s->pool.tick_steps(s->chunk, limit));
   if ((rc = cuda_check(cudaEventRecord(s->e0, s->st), "serve tick event"))) return rc;
   int64_t launched = 0;
   if ((rc = advance(s, n, k, &launched))) return rc;
@@ -322,6 +345,7 @@ int fsm_serve_stats(FsmServe* s, int64_t* stats, int32_t n) {
 
 int fsm_serve_destroy(FsmServe* s) {
   if (!s) return FSM_OK;
+  if (s->group) return set_error(FSM_ERR_INVALID, "serve_destroy: destroy the engine's group first");
   int rc;
   {
     std::lock_guard<std::mutex> g(s->mu);
@@ -331,6 +355,206 @@ int fsm_serve_destroy(FsmServe* s) {
     cudaEventDestroy(s->e1);
   }
   delete s;
+  return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Groups: engines of different grid sizes (and PDEs) ticked together on one stream. A group tick
+// admits into every member, advances every occupied slot of every member by the same k steps and
+// completes them together. Members whose plans are 1D lines of one nonlinear kind advance in ONE
+// launch (k_line_multi: a per-CTA table of (plan, first sample)); other members are launched one
+// after the other in the same tick (lockstep). Requests are still submitted to, polled from and
+// cancelled at the member engines.
+// ---------------------------------------------------------------------------
+struct FsmServeGroup {
+  std::vector<FsmServe*> m;
+  std::vector<int32_t> tick_n;  // occupied slots of each member in the tick in flight
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  bool in_flight = false;
+  bool line = false;  // every member a 1D line plan of one kind: one launch per tick
+  int kind = 0;
+  int32_t chunk = 0, tick_k = 0;
+  double tick_ms = 0.0;
+  double slot_step_ms = 0.0;  // device time per step and occupied slot, running mean over ticks
+  int64_t ticks = 0, launches = 0;
+  std::mutex mu;
+};
+
+namespace {
+
+bool line_member(const FsmServe* s) {
+  const FsmPlan* p = s->plan;
+  return p->path == 1 && p->n[0] >= 256 && p->n[0] <= 4096 &&
+         (p->nl == FSM_NL_KS || p->nl == FSM_NL_CONVECTION);
+}
+
+// Lock every member of the group, in member order (the only place that holds several).
+struct MemberLocks {
+  std::vector<std::unique_lock<std::mutex>> held;
+  explicit MemberLocks(FsmServeGroup* g) {
+    for (FsmServe* s : g->m) held.emplace_back(s->mu);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int fsm_serve_group_create(FsmServe* const* engines, int32_t count, double tick_ms, FsmServeGroup** out) {
+  if (!engines || !out || count < 1 || count > fsm::kLineMultiMax || tick_ms < 0.0)
+    return set_error(FSM_ERR_INVALID, "serve_group_create arguments (1 to 8 engines)");
+  for (int32_t i = 0; i < count; ++i) {
+    if (!engines[i] || engines[i]->group) return set_error(FSM_ERR_INVALID, "serve_group_create: engine missing or grouped");
+    for (int32_t j = 0; j < i; ++j)
+      if (engines[j] == engines[i]) return set_error(FSM_ERR_INVALID, "serve_group_create: engine listed twice");
+    if (engines[i]->st != engines[0]->st || engines[i]->device != engines[0]->device)
+      return set_error(FSM_ERR_INVALID, "serve_group_create: the engines must share one stream");
+    if (engines[i]->in_flight) return set_error(FSM_ERR_INVALID, "serve_group_create: an engine has a tick in flight");
+  }
+  FsmServeGroup* g = new FsmServeGroup();
+  g->m.assign(engines, engines + count);
+  g->tick_n.assign((size_t)count, 0);
+  g->st = engines[0]->st;
+  g->tick_ms = tick_ms;
+  g->chunk = engines[0]->chunk;
+  g->line = true;
+  g->kind = engines[0]->plan->nl;
+  for (FsmServe* s : g->m) {
+    g->chunk = std::min(g->chunk, s->chunk);
+    g->line = g->line && line_member(s) && s->plan->nl == g->kind;
+  }
+  int rc;
+  if ((rc = cuda_check(cudaEventCreate(&g->e0), "serve group event")) ||
+      (rc = cuda_check(cudaEventCreate(&g->e1), "serve group event"))) {
+    if (g->e0) cudaEventDestroy(g->e0);
+    delete g;
+    return rc;
+  }
+  for (FsmServe* s : g->m) {
+    std::lock_guard<std::mutex> l(s->mu);
+    s->group = g;
+  }
+  *out = g;
+  return FSM_OK;
+}
+
+int fsm_serve_group_tick(FsmServeGroup* g, int32_t* steps_launched) {
+  if (!g) return set_error(FSM_ERR_INVALID, "serve_group_tick arguments");
+  std::lock_guard<std::mutex> gl(g->mu);
+  MemberLocks locks(g);
+  if (steps_launched) *steps_launched = 0;
+  if (g->in_flight) return FSM_OK;
+  int rc;
+  int64_t total = 0;
+  for (FsmServe* s : g->m) {
+    if ((rc = admit(s))) return rc;
+    total += s->pool.occupied();
+  }
+  if (total == 0) return FSM_OK;
+  int32_t limit = 0;
+  if (g->slot_step_ms > 0.0 && g->tick_ms > 0.0)
+    limit = (int32_t)std::max(1.0, std::min(1e9, g->tick_ms / (g->slot_step_ms * (double)total)));
+  int32_t k = g->chunk;
+  for (FsmServe* s : g->m)
+    if (s->pool.occupied() > 0) k = std::min(k, s->pool.tick_steps(g->chunk, limit));
+  if ((rc = cuda_check(cudaEventRecord(g->e0, g->st), "serve group event"))) return rc;
+  int64_t launched = 0;
+  if (g->line) {
+    fsm::LineMulti lm;
+    memset(&lm, 0, sizeof(lm));
+    for (FsmServe* s : g->m) {
+      const int32_t n = s->pool.occupied();
+      if (n == 0) continue;
+      lm.a[lm.count] = fsm::base_args(s->plan, s->state, n, k);
+      lm.n[lm.count] = s->plan->n[0];
+      ++lm.count;
+    }
+    if ((rc = fsm::launch_line_multi(lm, g->kind, g->st))) return rc;
+    launched = 1;
+  } else {
+    k = graph_steps(g->m[0]->flags, k);
+    for (FsmServe* s : g->m) {
+      const int32_t n = s->pool.occupied();
+      if (n == 0) continue;
+      int64_t l = 0;
+      if ((rc = advance(s, n, k, &l))) return rc;
+      launched += l;
+    }
+  }
+  if ((rc = cuda_check(cudaEventRecord(g->e1, g->st), "serve group event"))) return rc;
+  for (size_t i = 0; i < g->m.size(); ++i) {
+    FsmServe* s = g->m[i];
+    const int32_t n = s->pool.occupied();
+    g->tick_n[i] = n;
+    if (n == 0) continue;
+    s->in_flight = true;
+    s->tick_k = k;
+    s->tick_n = n;
+    s->slot_steps += (int64_t)k * n;
+    ++s->ticks;
+  }
+  g->in_flight = true;
+  g->tick_k = k;
+  g->launches += launched;
+  ++g->ticks;
+  if (steps_launched) *steps_launched = k;
+  return FSM_OK;
+}
+
+int fsm_serve_group_poll(FsmServeGroup* g, int32_t wait, int32_t* in_flight) {
+  if (!g) return set_error(FSM_ERR_INVALID, "serve_group_poll arguments");
+  std::lock_guard<std::mutex> gl(g->mu);
+  if (in_flight) *in_flight = g->in_flight ? 1 : 0;
+  if (!g->in_flight) return FSM_OK;
+  cudaError_t q = wait ? cudaEventSynchronize(g->e1) : cudaEventQuery(g->e1);
+  if (q == cudaErrorNotReady) return FSM_OK;
+  int rc;
+  if ((rc = cuda_check(q, "serve group query"))) return rc;
+  float ms = 0.f;
+  if ((rc = cuda_check(cudaEventElapsedTime(&ms, g->e0, g->e1), "serve group time"))) return rc;
+  int64_t total = 0;
+  for (int32_t n : g->tick_n) total += n;
+  const double per = (double)ms / ((double)g->tick_k * (double)std::max<int64_t>(1, total));
+  g->slot_step_ms = g->slot_step_ms > 0.0 ? 0.5 * (g->slot_step_ms + per) : per;
+  MemberLocks locks(g);
+  g->in_flight = false;
+  for (size_t i = 0; i < g->m.size(); ++i) {
+    if (g->tick_n[i] == 0) continue;
+    if ((rc = complete_tick(g->m[i]))) return rc;
+  }
+  if (in_flight) *in_flight = 0;
+  return FSM_OK;
+}
+
+int fsm_serve_group_stats(FsmServeGroup* g, int64_t* stats, int32_t n) {
+  if (!g || !stats || n < 0) return set_error(FSM_ERR_INVALID, "serve_group_stats arguments");
+  std::lock_guard<std::mutex> gl(g->mu);
+  const int64_t v[FSM_SERVE_GROUP_NSTATS] = {g->ticks, g->launches, g->in_flight ? 1 : 0, g->line ? 1 : 0};
+  for (int32_t i = 0; i < n && i < FSM_SERVE_GROUP_NSTATS; ++i) stats[i] = v[i];
+  return FSM_OK;
+}
+
+int fsm_serve_group_destroy(FsmServeGroup* g) {
+  if (!g) return FSM_OK;
+  int rc;
+  {
+    std::lock_guard<std::mutex> gl(g->mu);
+    rc = cuda_check(cudaStreamSynchronize(g->st), "serve group destroy");
+    MemberLocks locks(g);
+    if (g->in_flight && !rc) {
+      // the device has finished the tick: account it, so that the members stay consistent
+      for (size_t i = 0; i < g->m.size() && !rc; ++i)
+        if (g->tick_n[i] > 0) rc = complete_tick(g->m[i]);
+      g->in_flight = false;
+    }
+    for (FsmServe* s : g->m) s->group = nullptr;
+    cudaEventDestroy(g->e0);
+    cudaEventDestroy(g->e1);
+  }
+  delete g;
   return rc;
 }
 

@@ -106,14 +106,15 @@ class _Bucket:
     spectrum and copies results to pinned host memory."""
 
     def __init__(self, kind: str, n: int, capacity: int, device: torch.device, chunk: int,
-                 priority: int = 0, tick_ms: float = 4.0, graphs: bool = True):
+                 priority: int = 0, tick_ms: float = 4.0, graphs: bool = True,
+                 stream: Optional[torch.cuda.Stream] = None):
         self.kind, self.n, self.capacity, self.device, self.chunk = kind, n, capacity, device, chunk
         op, mesh, C = problem(kind, n)
         self.C = C
         f_mesh = FourierMesh(mesh, device=device, dtype=torch.float32)
         op.register_mesh(f_mesh, C)
         prog = _native.lower(op._linear_terms, op._nonlinear_funcs, f_mesh, C, op._de_aliasing_rate)
-        self.stream = torch.cuda.Stream(device, priority=priority)
+        self.stream = stream if stream is not None else torch.cuda.Stream(device, priority=priority)
         with torch.cuda.stream(self.stream):
             self.plan = _native.NativePlan(prog, 0.05, _lib.FSM_SETDRK4, device,
                                            linear_coef64=op._linear_coef64(device), table_batch=capacity)
@@ -152,6 +153,11 @@ class _Bucket:
         if not self.in_flight:
             return []
         ids, self.in_flight = self.engine.poll(wait)
+        return self.finish(ids)
+
+    def finish(self, ids: List[int]) -> List[SolveRequest]:
+        """Turn the completed requests' half spectra into fields and start their copies to pinned host
+        memory on the bucket's stream."""
         done = []
         with torch.cuda.stream(self.stream):
             for rid in ids:
@@ -189,13 +195,64 @@ class _Bucket:
         return self.engine.stats()["graph_replays"]
 
 
+class _Group:
+    """Buckets ticked together by the library's serving group (``fsm_serve_group_*``): every tick
+    advances every occupied slot of every member by the same number of steps. The 1D KS buckets
+    (every grid size) form one group whose tick is ONE launch of the line kernel. The members share
+    one stream."""
+
+    def __init__(self, buckets: List[_Bucket], tick_ms: float):
+        self.buckets = buckets
+        self.stream = buckets[0].stream
+        self.group = _native.ServeGroup([b.engine for b in buckets], tick_ms=tick_ms)
+        self.in_flight = False
+
+    def feed(self, queues: Dict[Tuple[str, int], "collections.deque"], now: float) -> None:
+        for b in self.buckets:
+            b.feed(queues[(b.kind, b.n)], now)
+
+    def launch(self) -> int:
+        k = self.group.tick()
+        if k:
+            self.in_flight = True
+        return k
+
+    def poll(self, wait: bool = False) -> List[SolveRequest]:
+        if not self.in_flight:
+            return []
+        self.in_flight = self.group.poll(wait)
+        if self.in_flight:
+            return []
+        done = []
+        for b in self.buckets:
+            ids, _ = b.engine.poll(False)
+            done.extend(b.finish(ids))
+        return done
+
+    def close(self) -> None:
+        """Release the group (it waits for the stream); the members are closed by their owner."""
+        if self.group is not None:
+            self.group.close()
+            self.group = None
+
+    @property
+    def idle(self) -> bool:
+        return not self.in_flight and all(b.idle for b in self.buckets)
+
+    @property
+    def launches(self) -> int:
+        return self.group.stats()["launches"] if self.group is not None else 0
+
+
 class SolveServer:
     """Admission by HBM budget, per-bucket ticks on separate streams."""
 
     def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
-                 max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True, priority: str = "cheap"):
+                 max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True, priority: str = "cheap",
+                 group_lines: bool = True):
         """``priority``: which buckets get the high-priority streams, "cheap" (1D and 64^2 grids,
-        whose requests are short) or "costly" (the large 2D grids, whose requests are the long tail)."""
+        whose requests are short) or "costly" (the large 2D grids, whose requests are the long tail).
+        ``group_lines``: the 1D KS buckets of every grid size advance together, one launch per tick."""
         self.device = device
         self.graphs = graphs
         self.priority = priority
@@ -203,18 +260,35 @@ class SolveServer:
         self.chunk = chunk
         self.max_slots = max_slots
         self.tick_ms = tick_ms
+        self.group_lines = group_lines
         self.buckets: Dict[Tuple[str, int], _Bucket] = {}
+        self.groups: List[_Group] = []
 
     def prepare(self, keys: List[Tuple[str, int]], max_batch: int = 32) -> None:
-        """Create one bucket per (kind, n), splitting the HBM budget by footprint."""
+        """Create one bucket per (kind, n), splitting the HBM budget by footprint; the 1D KS buckets
+        (with ``group_lines``) share one stream and one serving group."""
         share = self.budget // max(1, len(keys))
         lo, hi = torch.cuda.Stream.priority_range()
+        line_keys = [k for k in keys if k[0] == "ks1d"] if self.group_lines else []
+        line_stream = None
+        if len(line_keys) > 1:
+            cheap_prio = hi if self.priority == "cheap" else lo
+            line_stream = torch.cuda.Stream(self.device, priority=cheap_prio)
         for kind, n in keys:
             cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
             cheap = kind == "ks1d" or n <= 64
             prio = hi if cheap == (self.priority == "cheap") else lo
-            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms, self.graphs)
+            stream = line_stream if (kind, n) in line_keys else None
+            self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms, self.graphs,
+                                              stream=stream)
+        if line_stream is not None:
+            self.groups.append(_Group([self.buckets[k] for k in sorted(line_keys, key=lambda k: k[1])], self.tick_ms))
         torch.cuda.synchronize(self.device)
+
+    def _units(self) -> list:
+        """What the host loop ticks: every group, and every bucket outside a group."""
+        grouped = {id(b) for g in self.groups for b in g.buckets}
+        return list(self.groups) + [b for b in self.buckets.values() if id(b) not in grouped]
 
     def run(self, requests: List[SolveRequest], realtime: bool = True) -> float:
         """Serve the requests (arrival times in seconds from start); returns the wall time."""
@@ -224,6 +298,7 @@ class SolveServer:
         if missing:
             self.prepare(missing)
         waiting: Dict[Tuple[str, int], collections.deque] = {k: collections.deque() for k in self.buckets}
+        units = self._units()
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0
         i, finished, total = 0, 0, len(pending)
@@ -242,12 +317,15 @@ class SolveServer:
                 else:
                     still.append(r)
             copying = still
-            for key, b in self.buckets.items():
-                copying.extend(b.poll())
-                b.feed(waiting[key], t)
-                if not b.in_flight:
-                    b.launch()
-                if b.in_flight:
+            for u in units:
+                copying.extend(u.poll())
+                if isinstance(u, _Group):
+                    u.feed(waiting, t)
+                else:
+                    u.feed(waiting[(u.kind, u.n)], t)
+                if not u.in_flight:
+                    u.launch()
+                if u.in_flight:
                     busy = True
             if not busy:
                 time.sleep(0.0001)
@@ -271,29 +349,33 @@ class SolveServer:
         device = self.device
         errors: List[BaseException] = []
 
-        def worker(key):
-            b = self.buckets[key]
-            q = queues[key]
+        def worker(u):
+            grouped = isinstance(u, _Group)
+            mine = [queues[(b.kind, b.n)] for b in u.buckets] if grouped else [queues[(u.kind, u.n)]]
             try:
                 with torch.cuda.device(device):
                     while True:
                         with cond:
-                            while not q and b.idle and not state["arrived"]:
+                            while not any(mine) and u.idle and not state["arrived"]:
                                 cond.wait(0.01)
-                            finished = state["arrived"] and not q and b.idle
+                            finished = state["arrived"] and not any(mine) and u.idle
                         if finished:
                             return
-                        b.feed(q, now())  # only this worker takes from q
-                        b.launch()
-                        if not b.in_flight:
+                        # only this worker takes from its queues
+                        if grouped:
+                            u.feed(queues, now())
+                        else:
+                            u.feed(mine[0], now())
+                        u.launch()
+                        if not u.in_flight:
                             continue
-                        for r in b.poll(wait=True):
+                        for r in u.poll(wait=True):
                             r._copied.synchronize()
                             r.t_done = now()
             except BaseException as e:  # surface worker failures to the caller
                 errors.append(e)
 
-        threads = [threading.Thread(target=worker, args=(k,), daemon=True) for k in self.buckets]
+        threads = [threading.Thread(target=worker, args=(u,), daemon=True) for u in self._units()]
         # No garbage collection while the workers run: a collection triggered in one worker runs
         # the finalizers of unreachable library objects there (plan destruction synchronises the
         # device and frees memory), while another worker may be capturing a tick's CUDA graph on its
@@ -328,7 +410,10 @@ class SolveServer:
         return now()
 
     def close(self) -> None:
-        """Release the buckets: each engine (it waits for its stream) before its plan."""
+        """Release the groups, then the buckets: each engine (it waits for its stream) before its plan."""
+        for g in self.groups:
+            g.close()
+        self.groups = []
         for b in self.buckets.values():
             b.close()
         self.buckets = {}
@@ -341,7 +426,7 @@ class SolveServer:
 
     @property
     def launches(self) -> int:
-        return sum(b.launches for b in self.buckets.values())
+        return sum(b.launches for b in self.buckets.values()) + sum(g.launches for g in self.groups)
 
     @property
     def graph_replays(self) -> int:

@@ -33,6 +33,7 @@ from __future__ import annotations
 import argparse
 import concurrent.futures as cf
 import ctypes
+import functools
 import json
 import math
 import os
@@ -94,14 +95,36 @@ def initial_vorticity(batch: int, seed: int = SEED) -> np.ndarray:
 # ---------------------------------------------------------------------------
 # CPU restatement of the reference (oracle), timed on the host cores
 # ---------------------------------------------------------------------------
+@functools.lru_cache(maxsize=1)
+def _cpu_port_step_setup():
+    """The oracle's mesh, nonlinear closure and SETDRK4 tables (complex64) of the headline workload."""
+    from oracle import spectral as S
+
+    mesh = S.OMesh(MESH, np.float32)
+    nonlinear = S.make_nonlinear(mesh, [(-1.0, "vorticity_convection")])
+    lin = S.linear_symbol(mesh, [(1.0 / RE, ("laplacian",))], 1)
+    tabs = S.build_tables("setdrk4", lin, DT)
+    tabs = {k: (v if k == "dt" else np.asarray(v).astype(mesh.complex_dtype if np.iscomplexobj(v) else mesh.real_dtype))
+            for k, v in tabs.items()}
+    return mesh, nonlinear, tabs
+
+
 def cpu_reference_throughput(samples: int, time_steps: int, threads: int) -> dict:
+    """The oracle's restatement of the reference's step (numpy complex64) on the host cores: the
+    mesh, the nonlinear closure and the SETDRK4 tables are built once, as the reference builds its
+    integrator once per (operator, mesh, dt); the timed region is ``time_steps`` steps of each of
+    ``samples`` fields, one field per thread."""
     from oracle import spectral as S
 
     w0 = initial_vorticity(samples, seed=SEED + 1)
+    mesh, nonlinear, tabs = _cpu_port_step_setup()
+    u_hat = [mesh.fft(w0[i : i + 1].astype(np.float32)) for i in range(samples)]
 
     def one(i):
-        S.integrate(w0[i : i + 1], MESH, [(1.0 / RE, ("laplacian",))], [(-1.0, "vorticity_convection")], DT,
-                    time_steps, real_dtype=np.float32)
+        u = u_hat[i]
+        for _ in range(time_steps):
+            u = S.stage_step("setdrk4", tabs, nonlinear, u)
+        return u
 
     t0 = time.perf_counter()
     with cf.ThreadPoolExecutor(max_workers=threads) as ex:
@@ -110,7 +133,7 @@ def cpu_reference_throughput(samples: int, time_steps: int, threads: int) -> dic
     dof_steps = samples * N * N * time_steps
     return {"value": dof_steps / elapsed, "unit": "DOF*steps/s", "cores": threads, "kind": "port",
             "sample": f"{samples} samples x {time_steps} SETDRK4 steps of the 256^2 workload "
-                      f"(numpy complex64 restatement, {threads} threads, coefficient build included)",
+                      f"(numpy complex64 restatement, {threads} threads; tables built once, outside the timing)",
             "seconds": elapsed}
 
 

@@ -612,8 +612,9 @@ def profile_kernels(plan, state0, ws, device) -> dict:
 
 
 # DRAM bytes of one column-pass launch at batch 64, from one ncu capture of `bench.py --ncu-case`
-# (dram__bytes_read.sum 35.1 MB + dram__bytes_write.sum 42.3 MB, stage 0 of a SETDRK4 step).
-COLUMN_PASS_DRAM_BYTES = 77.3e6
+# (dram__bytes_read.sum 36.5 MB + dram__bytes_write.sum 21.9 MB, stage 0 of a SETDRK4 step;
+# profiles/ns2d_vorticity_256x256_b64_plane_passes.md).
+COLUMN_PASS_DRAM_BYTES = 58.4e6
 
 
 HK = N // 3 + 1  # last-axis columns of the stage fields kept by the 2/3 rule (stored and read)
@@ -872,7 +873,7 @@ def run_serving(args):
         t_phase = now
 
     server = serving.SolveServer(device, hbm_budget_bytes=16 << 30, chunk=args.chunk, priority=args.priority,
-                                 group_lines=bool(args.group_lines))
+                                 group_lines=bool(args.group_lines), group_planes=bool(args.group_planes))
     server.prepare(sorted({(r.kind, r.n) for r in reqs}))
     # warm-up: a few requests through both paths (kernel attributes, plans of the plain path)
     warm = serving.make_stream(8, seed=99, rate_hz=0.0, max_steps=120)
@@ -1103,6 +1104,48 @@ def ncu_case(workload: str = "ns2d", n3d: int = 256):
         torch.cuda.synchronize()
         print("ncu case done", bool(torch.isfinite(u.grad).all().item()))
         return
+    if workload == "serving":
+        # the serving groups' kernels: KS 1D at 256, 1024 and 4096 points advanced by one line launch
+        # per tick (k_line_multi), 2D Burgers at 64^2, 128^2 and 256^2 by one launch per pass
+        # (k_axis0_multi2, k_plane_row_multi); 8 requests per size, 16 slots per engine, ticks of 8 steps
+        from torchfsm_gb300 import _lib, _native, serving
+        from torchfsm_gb300.mesh import FourierMesh
+
+        device = torch.device("cuda", 0)
+        groups, keep = [], []
+        for kind, sizes in (("ks1d", (256, 1024, 4096)), ("burgers2d", (64, 128, 256))):
+            stream = torch.cuda.Stream(device)
+            pools = []
+            for n in sizes:
+                op, mesh, C = serving.problem(kind, n)
+                f_mesh = FourierMesh(mesh, device=device, dtype=torch.float32)
+                op.register_mesh(f_mesh, C)
+                prog = _native.lower(op._linear_terms, op._nonlinear_funcs, f_mesh, C, op._de_aliasing_rate)
+                with torch.cuda.stream(stream):
+                    plan = _native.NativePlan(prog, 0.05, _lib.FSM_SETDRK4, device,
+                                              linear_coef64=op._linear_coef64(device), table_batch=16)
+                torch.cuda.synchronize()
+                pool = _native.ServePool(plan, 16, 8, stream)
+                shape = (n,) if kind == "ks1d" else (n, n)
+                for rid in range(8):
+                    u = initial.band_limited(shape, 2, C, 8, SEED + rid, 1.0 if kind == "ks1d" else 0.25)
+                    h = _native.Spectral(plan).to_half(torch.tensor(u, dtype=torch.float32, device=device)).contiguous()
+                    pool.submit(rid, 32, 0.02, h)
+                    keep.append(h)
+                pools.append(pool)
+            groups.append((_native.ServeGroup(pools, tick_ms=0.0), pools))
+        torch.cuda.synchronize()
+        for group, pools in groups:
+            for _ in range(4):
+                group.tick()
+                group.poll(wait=True)
+                for p in pools:
+                    p.poll(False)
+        torch.cuda.synchronize()
+        print("ncu case done", all(bool(torch.isfinite(torch.view_as_real(h)).all()) for h in keep))
+        for group, pools in groups:
+            group.close()
+        return
     if workload in ("burgers1d", "ks1d", "heat2d"):
         # the kernels outside the plane and volume passes, on small cases of their workloads:
         # burgers1d: the 1D line kernel at N = 128 (200 steps, 201 frames), the FP64 coefficient kernel
@@ -1201,7 +1244,7 @@ def other_workloads(args) -> dict:
                                                                      "reference_autograd.rel_l2_grad_u0_vs_adjoint",
                                                                      "reference_autograd.rel_diff_grad_nu_vs_adjoint"]),
     }
-    serve = _ap.Namespace(**dict(vars(args), requests=args.serve_summary_requests, loads=str(args.load),
+    serve = _ap.Namespace(**dict(vars(args), requests=args.serve_summary_requests, loads=args.loads,
                                  ref_requests=0, ref_cpu_requests=0))
     if args.serve_summary_requests > 0:
         legs[f"serving_{args.serve_summary_requests}_requests"] = (
@@ -1244,11 +1287,12 @@ def fused_line(res: dict, args, world: int, cpu: Optional[dict], ref_cpu: Option
                 "d2h_bytes_per_step": res["d2h"], "ms_per_step": res["e2e_ms"],
                 "first_call_with_build_ms": res["first_ms"]},
         "gpu_launches": res["launches"] * args.steps,
-        "roofline": {"bound": "hbm", "kernel": "k_axis0_r<256, VORTICITY, 2> (column pass)",
+        "roofline": {"bound": "hbm", "kernel": "k_axis0_r2<256, VORTICITY, 2> (column pass, SETDRK4 stages)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": COLUMN_PASS_DRAM_BYTES,
                      "traffic_note": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one stage-0 column pass "
-                                     "launch of this workload (bench.py --ncu-case)",
+                                     "launch of this workload (bench.py --ncu-case; "
+                                     "profiles/ns2d_vorticity_256x256_b64_plane_passes.md)",
                      "peak_source": f"{peak_kind} hbm_gbs",
                      "per_kernel_ms": {k: v["avg_ms"] for k, v in res["prof"].items() if v["launches"]},
                      "step_model_bytes_per_dof_step": step_model_bytes_per_dof_step(),
@@ -1284,20 +1328,22 @@ def main():
     ap.add_argument("--no-fp64-reference", action="store_true",
                     help="skip the accuracy leg (the reference's float64 run of the first samples)")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
-    ap.add_argument("--loads", default="0.35,0.5",
+    ap.add_argument("--loads", default="0.25,0.35",
                     help="serving: Poisson rates measured, as fractions of the burst capacity")
     ap.add_argument("--chunk", type=int, default=50, help="serving: steps per tick")
     ap.add_argument("--ref-requests", type=int, default=20,
                     help="serving: requests of the stream run by the reference's torch GPU path")
     ap.add_argument("--ref-cpu-requests", type=int, default=3,
                     help="serving: requests of the stream run by the reference's CPU path")
-    ap.add_argument("--load", type=float, default=0.35, help="serving: the Poisson rate whose figures head the line, as a fraction of capacity")
+    ap.add_argument("--load", type=float, default=0.25, help="serving: the Poisson rate whose figures head the line, as a fraction of capacity")
     ap.add_argument("--threaded", type=int, default=1, help="serving: one host worker thread per bucket")
     ap.add_argument("--serve-summary-requests", type=int, default=2000,
                     help="ns2d: requests of the serving stream summarised on the headline line after its timed "
-                         "region (burst, plain path, one Poisson load; 0: skip)")
+                         "region (burst, plain path, the --loads Poisson rates; 0: skip)")
     ap.add_argument("--group-lines", type=int, default=1,
                     help="serving: the 1D KS buckets of every size advance together, one launch per tick")
+    ap.add_argument("--group-planes", type=int, default=0,
+                    help="serving: the 2D Burgers buckets of every size advance together, one launch per pass")
     ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],
                     help="serving: buckets on the high-priority streams")
     ap.add_argument("--workload", default="ns2d",

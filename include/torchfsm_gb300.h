@@ -308,16 +308,20 @@ int fsm_serve_destroy(FsmServe* server);
  *   member by the same k steps (the fewest remaining steps of any active request, at most the
  *   smallest member chunk and the tick_ms bound). When every member is a 1D line plan of 256 to
  *   4096 points and one nonlinear kind (KS or Burgers), the tick is ONE kernel launch over all
- *   of them; otherwise the members are launched one after the other in the tick (lockstep).
+ *   of them. When every member is a SETDRK4 plan of a square 2D grid of 64, 128 or 256 points
+ *   per axis and one nonlinear kind (Convection or VorticityConvection), each pass of the tick
+ *   is one launch over all of them (a priming column pass, then a row and a column pass per
+ *   stage). Otherwise the members are launched one after the other in the tick (lockstep).
  *   *steps_launched = k, 0 when a tick is in flight or no slot is occupied.
  * fsm_serve_group_poll: complete the group's tick once the device has finished it (wait != 0:
  *   block until then): every member's finished requests leave as in fsm_serve_poll;
  *   *in_flight = 1 while the tick is still running.
- * fsm_serve_group_stats: up to n of {ticks, kernel launches, tick in flight, one launch per tick}.
+ * fsm_serve_group_stats: up to n of {ticks, kernel launches, tick in flight, one launch per tick
+ *   (1D lines), one launch per pass (2D planes)}.
  * fsm_serve_group_destroy: waits for the stream, accounts a finished tick, releases the members
  *   (which may then be ticked alone or destroyed; destroying a member of a group is refused). */
 typedef struct FsmServeGroup FsmServeGroup;
-#define FSM_SERVE_GROUP_NSTATS 4
+#define FSM_SERVE_GROUP_NSTATS 5
 int fsm_serve_group_create(FsmServe* const* engines, int32_t count, double tick_ms, FsmServeGroup** out);
 int fsm_serve_group_tick(FsmServeGroup* group, int32_t* steps_launched);
 int fsm_serve_group_poll(FsmServeGroup* group, int32_t wait, int32_t* in_flight);

@@ -220,10 +220,10 @@ def test_other_workloads_summaries_and_failures(monkeypatch):
     monkeypatch.setattr(bench, "run_burgers2d_grad", broken)
     monkeypatch.setattr(bench, "run_serving", fake_serving)
     out = bench.other_workloads(argparse.Namespace(steps=20, warmup=5, no_fp64_reference=False,
-                                                   serve_summary_requests=300, load=0.35))
+                                                   serve_summary_requests=300, load=0.25, loads="0.25,0.35"))
     serve = out["serving_300_requests"]
     assert serve["value"] == 5.0 and serve["serving.speedup_vs_plain"] == 3.2 and serve["serving.latency_s"] == {"p99": 0.8}
-    assert seen["serve"] == (300, "0.35", 0, 0)  # one Poisson load, no reference samples
+    assert seen["serve"] == (300, "0.25,0.35", 0, 0)  # the Poisson loads, no reference samples
     one = out["burgers1d_n128_200steps"]
     assert one["value"] == 1.0 and one["latency_ms"] == {"p50": 2.0} and one["config.rel_l2_traj_vs_fp64"] == 3e-7
     assert one["torch_gpu_reference.latency_ms"] is None and one["wall_s"] >= 0

@@ -1,5 +1,6 @@
 """Serving groups (fsm_serve_group_*): engines of different grid sizes ticked together. The 1D KS
-engines of every size advance in ONE launch per tick (k_line_multi); 2D engines tick in lockstep.
+engines of every size advance in ONE launch per tick (k_line_multi); 2D engines of square grids
+in one launch per pass (k_axis0_multi2 / k_plane_row_multi); other mixes tick in lockstep.
 Each request's result equals a plain integration of its samples, and served KS solves match the
 reference's FP64 runs (golden fixtures)."""
 
@@ -126,8 +127,9 @@ def test_line_group_serves_reference_fp64_solutions():
     pool5.__del__()
 
 
-def test_group_2d_lockstep_matches_plain_integration():
-    """2D Burgers at 64^2 and 128^2 ticked in lockstep by one group (one stream)."""
+def test_group_2d_one_launch_per_pass_matches_plain_integration():
+    """2D Burgers at 64^2 and 128^2 advanced by one group: each column and row pass of a tick is one
+    launch over both sizes (a priming pass, then two launches per stage)."""
     stream = torch.cuda.Stream(DEV)
     eng = {n: _engine("burgers2d", n, capacity=6, chunk=8, stream=stream) for n in (64, 128)}
     group = _native.ServeGroup([eng[n][3] for n in (64, 128)], tick_ms=0.0)
@@ -143,7 +145,31 @@ def test_group_2d_lockstep_matches_plain_integration():
     for rid in halves:
         assert _rel(halves[rid], refs[rid]) <= 1e-6, rid
     st = group.stats()
-    assert st["one_launch"] == 0 and st["launches"] > st["ticks"]
+    assert st["one_launch"] == 0 and st["one_launch_per_pass"] == 1
+    # every tick: one priming launch and 2 launches per stage of each of its k steps
+    assert st["launches"] > st["ticks"] and (st["launches"] - st["ticks"]) % 8 == 0
+    group.close()
+
+
+def test_group_of_mixed_kinds_ticks_in_lockstep():
+    """A 1D KS engine and a 2D Burgers engine in one group: no shared kernel, so the members launch one
+    after the other in each tick; results are unchanged."""
+    stream = torch.cuda.Stream(DEV)
+    ks = _engine("ks1d", 256, capacity=4, chunk=8, stream=stream)
+    bg = _engine("burgers2d", 64, capacity=4, chunk=8, stream=stream)
+    group = _native.ServeGroup([ks[3], bg[3]], tick_ms=0.0)
+    halves, refs = {}, {}
+    for rid, (eng, kind, n, b, steps, dt) in enumerate([(ks, "ks1d", 256, 3, 17, 0.05),
+                                                        (bg, "burgers2d", 64, 2, 13, 0.03)]):
+        prog, L, plan, pool = eng
+        halves[rid] = _half(plan, kind, n, b, 700 + rid)
+        refs[rid] = _plain(prog, L, halves[rid], steps, dt)
+        pool.submit(rid, steps, dt, halves[rid])
+    _drain(group, [ks[3], bg[3]])
+    for rid in halves:
+        assert _rel(halves[rid], refs[rid]) <= 1e-6, rid
+    st = group.stats()
+    assert st["one_launch"] == 0 and st["one_launch_per_pass"] == 0
     group.close()
 
 

@@ -384,12 +384,13 @@ class ServePool:
 
 class ServeGroup:
     """Serving engines of different grid sizes ticked together (``fsm_serve_group_*``): one tick
-    advances every occupied slot of every member by the same number of steps, as ONE kernel
-    launch when every member is a 1D line plan of one nonlinear kind, else the members one after
-    the other. The members share one stream; requests are still submitted to and polled from
+    advances every occupied slot of every member by the same number of steps: as ONE kernel
+    launch when every member is a 1D line plan of one nonlinear kind, with one launch per pass
+    when every member is a square 2D plan (64, 128, 256) of one nonlinear kind, else the members
+    one after the other. The members share one stream; requests are still submitted to and polled from
     them. Close the group before its members."""
 
-    STATS = ("ticks", "launches", "in_flight", "one_launch")
+    STATS = ("ticks", "launches", "in_flight", "one_launch", "one_launch_per_pass")
 
     def __init__(self, pools: List[ServePool], tick_ms: float = 0.0):
         self.pools = list(pools)

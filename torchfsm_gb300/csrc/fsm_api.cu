@@ -743,6 +743,26 @@ StepArgs batch_arrays(const FsmPlan* p, StepArgs a, float2* arr, int b0, int n) 
   return a;
 }
 
+}  // namespace
+
+namespace fsm {
+int plane_args(const FsmPlan* p, void* state, int32_t batch, int32_t steps, void* workspace, size_t workspace_bytes,
+               StepArgs* out) {
+  if (!p || !state || !workspace || !out || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "plane_args");
+  if (p->path != 2) return set_error(FSM_ERR_INVALID, "plane_args: not a 2D plane-pass plan");
+  size_t off_arrays = 0;
+  if (workspace_bytes < workspace_layout(p, batch, steps, &off_arrays))
+    return set_error(FSM_ERR_INVALID, "plane_args: workspace too small");
+  char* ws = (char*)workspace;
+  StepArgs a = base_args(p, state, batch, steps);
+  a.dc = (float2*)(ws + align256((size_t)(steps + 1) * sizeof(int32_t)));
+  *out = batch_arrays(p, a, (float2*)(ws + off_arrays), 0, batch);
+  return FSM_OK;
+}
+}  // namespace fsm
+
+namespace {
+
 // The launch sequence of the plane (2D) / volume (3D) passes, step by step: prime() before
 // the first step, then step(k) for k = 0 .. steps-1, on one stream.
 struct PlaneSequence {

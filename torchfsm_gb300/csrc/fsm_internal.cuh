@@ -89,6 +89,25 @@ struct LineMulti {
   int32_t count;
 };
 int launch_line_multi(LineMulti& m, int kind, cudaStream_t st);
+
+// One launch of the 2D register column (or row) pass over the samples of several plans of square
+// grids (64, 128 or 256 points per axis, Convection or VorticityConvection): entry j runs the pass
+// on a[j].B samples of a[j] (arguments of plane_args, stage and emit set by the caller). gx and
+// cta0 are filled in by the launchers. fast: the SETDRK4 stage launch (stage >= 0).
+constexpr int kPlaneMultiMax = 8;
+struct PlaneMulti {
+  StepArgs a[kPlaneMultiMax];
+  int32_t n[kPlaneMultiMax];
+  int32_t gx[kPlaneMultiMax];
+  int32_t cta0[kPlaneMultiMax + 1];
+  int32_t count;
+};
+int launch_plane_col_multi(PlaneMulti& m, int kind, bool fast, cudaStream_t st);
+int launch_plane_row_multi(PlaneMulti& m, int kind, cudaStream_t st);
+// The plane passes' arguments for `batch` samples of `state` advanced by `steps` steps without
+// recording, with the pass arrays in `workspace` laid out as fsm_integrate lays them out (fsm_api.cu).
+int plane_args(const FsmPlan* p, void* state, int32_t batch, int32_t steps, void* workspace, size_t workspace_bytes,
+               StepArgs* out);
 // Register-FFT plane passes (64..256 points per axis); return -1 when no kernel covers the sizes.
 int launch_plane_col_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);
 int launch_plane_row_reg(const FsmPlan* p, const StepArgs& a, cudaStream_t st);

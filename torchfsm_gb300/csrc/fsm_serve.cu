@@ -374,7 +374,8 @@ struct FsmServeGroup {
   cudaStream_t st = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   bool in_flight = false;
-  bool line = false;  // every member a 1D line plan of one kind: one launch per tick
+  bool line = false;   // every member a 1D line plan of one kind: one launch per tick
+  bool plane = false;  // every member a square 2D register-pass plan of one kind: one launch per pass
   int kind = 0;
   int32_t chunk = 0, tick_k = 0;
   double tick_ms = 0.0;
@@ -389,6 +390,48 @@ bool line_member(const FsmServe* s) {
   const FsmPlan* p = s->plan;
   return p->path == 1 && p->n[0] >= 256 && p->n[0] <= 4096 &&
          (p->nl == FSM_NL_KS || p->nl == FSM_NL_CONVECTION);
+}
+
+bool plane_member(const FsmServe* s) {
+  const FsmPlan* p = s->plan;
+  const int n = p->n[0];
+  return p->path == 2 && p->ndim == 2 && p->n[1] == n && (n == 64 || n == 128 || n == 256) &&
+         (p->nl == FSM_NL_CONVECTION || p->nl == FSM_NL_VORTICITY) && p->integ == FSM_SETDRK4 &&
+         (p->hk == n / 3 + 1 || p->hk == n / 2 + 1);
+}
+
+// k SETDRK4 steps of the occupied slots of every member: a priming column pass, then per stage
+// one row pass and one column pass, each a single launch over all members (fsm_plane_multi.cu).
+int plane_tick(FsmServeGroup* g, int32_t k, int64_t* launched) {
+  fsm::PlaneMulti pm;
+  memset(&pm, 0, sizeof(pm));
+  int rc;
+  for (FsmServe* s : g->m) {
+    const int32_t n = s->pool.occupied();
+    if (n == 0) continue;
+    if ((rc = fsm::plane_args(s->plan, s->state, n, k, s->ws, s->ws_bytes, &pm.a[pm.count]))) return rc;
+    pm.n[pm.count] = s->plan->n[0];
+    ++pm.count;
+  }
+  for (int j = 0; j < pm.count; ++j) {
+    pm.a[j].stage = -1;
+    pm.a[j].emit = 1;
+  }
+  if ((rc = fsm::launch_plane_col_multi(pm, g->kind, false, g->st))) return rc;
+  *launched = 1;
+  const int ns = g->m[0]->plan->nstages;
+  for (int32_t step = 0; step < k; ++step) {
+    for (int st = 0; st < ns; ++st) {
+      if ((rc = fsm::launch_plane_row_multi(pm, g->kind, g->st))) return rc;
+      for (int j = 0; j < pm.count; ++j) {
+        pm.a[j].stage = st;
+        pm.a[j].emit = !(st == ns - 1 && step == k - 1);
+      }
+      if ((rc = fsm::launch_plane_col_multi(pm, g->kind, true, g->st))) return rc;
+      *launched += 2;
+    }
+  }
+  return FSM_OK;
 }
 
 // Lock every member of the group, in member order (the only place that holds several).
@@ -421,10 +464,12 @@ int fsm_serve_group_create(FsmServe* const* engines, int32_t count, double tick_
   g->tick_ms = tick_ms;
   g->chunk = engines[0]->chunk;
   g->line = true;
+  g->plane = true;
   g->kind = engines[0]->plan->nl;
   for (FsmServe* s : g->m) {
     g->chunk = std::min(g->chunk, s->chunk);
     g->line = g->line && line_member(s) && s->plan->nl == g->kind;
+    g->plane = g->plane && plane_member(s) && s->plan->nl == g->kind;
   }
   int rc;
   if ((rc = cuda_check(cudaEventCreate(&g->e0), "serve group event")) ||
@@ -474,6 +519,8 @@ int fsm_serve_group_tick(FsmServeGroup* g, int32_t* steps_launched) {
     }
     if ((rc = fsm::launch_line_multi(lm, g->kind, g->st))) return rc;
     launched = 1;
+  } else if (g->plane) {
+    if ((rc = plane_tick(g, k, &launched))) return rc;
   } else {
     k = graph_steps(g->m[0]->flags, k);
     for (FsmServe* s : g->m) {
@@ -532,7 +579,8 @@ int fsm_serve_group_poll(FsmServeGroup* g, int32_t wait, int32_t* in_flight) {
 int fsm_serve_group_stats(FsmServeGroup* g, int64_t* stats, int32_t n) {
   if (!g || !stats || n < 0) return set_error(FSM_ERR_INVALID, "serve_group_stats arguments");
   std::lock_guard<std::mutex> gl(g->mu);
-  const int64_t v[FSM_SERVE_GROUP_NSTATS] = {g->ticks, g->launches, g->in_flight ? 1 : 0, g->line ? 1 : 0};
+  const int64_t v[FSM_SERVE_GROUP_NSTATS] = {g->ticks, g->launches, g->in_flight ? 1 : 0, g->line ? 1 : 0,
+                                            g->plane ? 1 : 0};
   for (int32_t i = 0; i < n && i < FSM_SERVE_GROUP_NSTATS; ++i) stats[i] = v[i];
   return FSM_OK;
 }

@@ -198,8 +198,9 @@ class _Bucket:
 class _Group:
     """Buckets ticked together by the library's serving group (``fsm_serve_group_*``): every tick
     advances every occupied slot of every member by the same number of steps. The 1D KS buckets
-    (every grid size) form one group whose tick is ONE launch of the line kernel. The members share
-    one stream."""
+    (every grid size) form one group whose tick is ONE launch of the line kernel; the 2D Burgers
+    buckets (64^2, 128^2, 256^2) one group whose column and row passes are one launch each per
+    stage. The members share one stream."""
 
     def __init__(self, buckets: List[_Bucket], tick_ms: float):
         self.buckets = buckets
@@ -249,10 +250,11 @@ class SolveServer:
 
     def __init__(self, device: torch.device, hbm_budget_bytes: int = 8 << 30, chunk: int = 50,
                  max_slots: int = 256, tick_ms: float = 4.0, graphs: bool = True, priority: str = "cheap",
-                 group_lines: bool = True):
+                 group_lines: bool = True, group_planes: bool = False):
         """``priority``: which buckets get the high-priority streams, "cheap" (1D and 64^2 grids,
         whose requests are short) or "costly" (the large 2D grids, whose requests are the long tail).
-        ``group_lines``: the 1D KS buckets of every grid size advance together, one launch per tick."""
+        ``group_lines``: the 1D KS buckets of every grid size advance together, one launch per tick.
+        ``group_planes``: the 2D Burgers buckets of every grid size tick together on one stream."""
         self.device = device
         self.graphs = graphs
         self.priority = priority
@@ -261,6 +263,7 @@ class SolveServer:
         self.max_slots = max_slots
         self.tick_ms = tick_ms
         self.group_lines = group_lines
+        self.group_planes = group_planes
         self.buckets: Dict[Tuple[str, int], _Bucket] = {}
         self.groups: List[_Group] = []
 
@@ -270,19 +273,22 @@ class SolveServer:
         share = self.budget // max(1, len(keys))
         lo, hi = torch.cuda.Stream.priority_range()
         line_keys = [k for k in keys if k[0] == "ks1d"] if self.group_lines else []
-        line_stream = None
+        plane_keys = [k for k in keys if k[0] == "burgers2d"] if self.group_planes else []
+        shared = {}
         if len(line_keys) > 1:
-            cheap_prio = hi if self.priority == "cheap" else lo
-            line_stream = torch.cuda.Stream(self.device, priority=cheap_prio)
+            shared["line"] = torch.cuda.Stream(self.device, priority=hi if self.priority == "cheap" else lo)
+        if len(plane_keys) > 1:
+            shared["plane"] = torch.cuda.Stream(self.device, priority=lo if self.priority == "cheap" else hi)
         for kind, n in keys:
             cap = int(min(self.max_slots, max(max_batch, share // slot_bytes(kind, n, self.chunk))))
             cheap = kind == "ks1d" or n <= 64
             prio = hi if cheap == (self.priority == "cheap") else lo
-            stream = line_stream if (kind, n) in line_keys else None
+            stream = shared.get("line") if (kind, n) in line_keys else shared.get("plane") if (kind, n) in plane_keys else None
             self.buckets[(kind, n)] = _Bucket(kind, n, cap, self.device, self.chunk, prio, self.tick_ms, self.graphs,
                                               stream=stream)
-        if line_stream is not None:
-            self.groups.append(_Group([self.buckets[k] for k in sorted(line_keys, key=lambda k: k[1])], self.tick_ms))
+        for name, ks in (("line", line_keys), ("plane", plane_keys)):
+            if name in shared:
+                self.groups.append(_Group([self.buckets[k] for k in sorted(ks, key=lambda k: k[1])], self.tick_ms))
         torch.cuda.synchronize(self.device)
 
     def _units(self) -> list:

@@ -447,7 +447,37 @@ GENERIC_GRAD_CASES = {
         ic=_bl(303, (64,), 4, 0.5),
         build=lambda M, c: c * M.operator.SpatialDerivative(0, 3) + 6.0 * M.operator.Convection(),
     ),
+    # other integrators: the recomputed segments step with the scheme's own recurrence and tables
+    "grad_burgers1d_etdrk2_n64": dict(
+        mesh=[(0, TWO_PI, 64)], batch=2, channels=1, dt=0.01, step=30, coef=0.05, coef_target=0.08,
+        ic=_bl(304, (64,), 4, 0.5), integrator="etdrk2",
+        build=lambda M, c: c * M.operator.Laplacian() - M.operator.Convection(),
+    ),
+    "grad_burgers2d_setdrk3_n32": dict(
+        mesh=[(0, TWO_PI, 32), (0, TWO_PI, 32)], batch=2, channels=2, dt=0.01, step=20, coef=0.05,
+        coef_target=0.08, ic=_bl(305, (32, 32), 4, 0.5), integrator="setdrk3",
+        build=lambda M, c: c * M.operator.Laplacian() - M.operator.Convection(),
+    ),
+    "grad_burgers1d_rk4_n64": dict(
+        mesh=[(0, TWO_PI, 64)], batch=2, channels=1, dt=0.005, step=30, coef=0.05, coef_target=0.08,
+        ic=_bl(306, (64,), 4, 0.5), integrator="RK4",
+        build=lambda M, c: c * M.operator.Laplacian() - M.operator.Convection(),
+    ),
+    "grad_heat2d_etdrk0_n16": dict(
+        mesh=[(0, TWO_PI, 16), (0, TWO_PI, 16)], batch=2, channels=1, dt=0.05, step=10, coef=0.1,
+        coef_target=0.15, ic=_bl(307, (16, 16), 4, 1.0),
+        build=lambda M, c: c * M.operator.Laplacian(),
+    ),
 }
+
+
+def build_generic_grad_op(name: str, M, coef):
+    """The operator of a generic gradient case with its coefficient and integrator."""
+    case = GENERIC_GRAD_CASES[name]
+    op = case["build"](M, coef)
+    if case.get("integrator"):
+        set_case_integrator(op, M, case["integrator"])
+    return op
 
 
 def generic_grad_initial_condition(name: str) -> np.ndarray:

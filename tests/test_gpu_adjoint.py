@@ -145,7 +145,7 @@ def test_recomputed_segments_match_reference_autograd(name):
     dev = torch.device("cuda", 0)
     M = C.namespace("torchfsm_gb300")
     coef = torch.tensor(case["coef"], dtype=torch.float32, device=dev, requires_grad=True)
-    op = case["build"](M, coef)
+    op = C.build_generic_grad_op(name, M, coef)
     u0 = torch.tensor(g["u0"], dtype=torch.float32, device=dev, requires_grad=True)
     target = torch.tensor(g["target"], dtype=torch.float32, device=dev)
     out = op.integrate(u_0=u0, mesh=case["mesh"], dt=case["dt"], step=case["step"])
@@ -157,6 +157,6 @@ def test_recomputed_segments_match_reference_autograd(name):
     # 1e-4, or twice the reference's own float32 autograd error where that floor is higher (KdV: the
     # i k^3 symbol amplifies every step's rounding; the reference's FP32 gradient is 1.9e-4 off)
     tol_u = max(1e-4, 2 * float(g["fp32_grad_u0_rel_l2"]))
-    tol_c = max(1e-4, 2 * float(g["fp32_grad_coef_rel"]))
+    tol_c = max(1e-4, 2 * float(np.nan_to_num(g["fp32_grad_coef_rel"])))  # NaN: the float32 autograd is NaN
     print(f"{name}: grad u0 rel-L2 {err_u:.2e} (bound {tol_u:.1e}), grad coef rel {err_c:.2e} (bound {tol_c:.1e})")
     assert err_u <= tol_u and err_c <= tol_c

@@ -38,6 +38,10 @@ _GENERIC_TERMS = {
     "grad_ns2d_n32": lambda c: ([(c, ("laplacian",))], [(-1.0, "vorticity_convection")]),
     "grad_ksnd2d_n32": lambda c: ([(c, ("laplacian",)), (-1.0, ("biharmonic",))], [(-1.0, "ks_convection")]),
     "grad_kdv1d_n64": lambda c: ([(c, ("spatial_derivative", 0, 3))], [(6.0, "convection")]),
+    "grad_burgers1d_etdrk2_n64": lambda c: ([(c, ("laplacian",))], [(-1.0, "convection")]),
+    "grad_burgers2d_setdrk3_n32": lambda c: ([(c, ("laplacian",))], [(-1.0, "convection")]),
+    "grad_burgers1d_rk4_n64": lambda c: ([(c, ("laplacian",))], [(-1.0, "convection")]),
+    "grad_heat2d_etdrk0_n16": lambda c: ([(c, ("laplacian",))], []),
 }
 
 
@@ -45,7 +49,9 @@ def _generic_loss(name, u0, coef):
     c = C.GENERIC_GRAD_CASES[name]
     g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
     lin, nl = _GENERIC_TERMS[name](coef)
-    out, _ = S.integrate(u0, c["mesh"], lin, nl, c["dt"], c["step"])
+    integ = c.get("integrator", "auto")
+    out, _ = S.integrate(u0, c["mesh"], lin, nl, c["dt"], c["step"], integrator=integ if integ in S.RK_TABLEAUS
+                         else integ.lower())
     return float(np.mean((out - g["target"]) ** 2))
 
 

@@ -42,6 +42,7 @@ import math
 import torch
 
 from . import _lib, _native
+from .integrator._standalone import RK_TABLES as _RK_TABLES
 
 
 def _contour_tables(L: torch.Tensor, dt: float, M: int = 16, r: float = 1.0):
@@ -300,47 +301,108 @@ class _IntegrateFn(torch.autograd.Function):
         return (grad_u0, None, None, None, None, *grads)
 
 
-def _contour_tables_complex(L: torch.Tensor, dt: float, M: int, r: float):
-    """E, E2 (complex) and c1, c4, c5, c6 (their real parts, as the reference keeps them) of SETDRK4
-    for a complex128 symbol L, in torch arithmetic that autograd differentiates with respect to L
-    (integrator/_stable_etdrk/_uncached.py:8-43, 180-211)."""
+def _scheme_tables(scheme: int, L: torch.Tensor, dt: float, M: int, r: float) -> dict:
+    """The coefficient tables of an integration scheme as torch functions of the complex128 symbol L,
+    which autograd differentiates with respect to L (and so to the coefficients in L).
+
+    SETDRK1-4: the means over M contour points z = r e^{i pi (2j-1)/M} + dt L of the reference's
+    integrands, real parts kept (integrator/_stable_etdrk/_uncached.py:8-43, 46-211); ETDRK0-2: the
+    closed forms with their L == 0 limits, complex (integrator/_etdrk.py:10-82; the limits are
+    selected without the 0/0 of the other branch, so their gradients stay finite); Runge-Kutta: the
+    symbol itself (the slopes are dt (L x + N(x)), operator/_base.py:408-431)."""
+    if scheme in _RK_TABLES:
+        return {"L": L}
+    E = torch.exp(dt * L)
+    if scheme in (_lib.FSM_ETDRK0, _lib.FSM_ETDRK1, _lib.FSM_ETDRK2):
+        out = {"E": E}
+        zero = L == 0
+        Ls = torch.where(zero, torch.ones_like(L), L)
+        if scheme != _lib.FSM_ETDRK0:
+            out["c1"] = torch.where(zero, torch.full_like(L, dt), (E - 1) / Ls)
+        if scheme == _lib.FSM_ETDRK2:
+            out["c2"] = torch.where(zero, torch.full_like(L, dt / 2), (E - 1 - Ls * dt) / (Ls ** 2 * dt))
+        return out
     j = torch.arange(1, M + 1, device=L.device, dtype=torch.float64)
     roots = torch.exp(2j * math.pi * (j - 0.5) / M)
     z = r * roots + (L * dt).unsqueeze(-1)
     ez = torch.exp(z)
-    E = torch.exp(dt * L)
-    E2 = torch.exp(0.5 * dt * L)
-    c1 = dt * ((torch.exp(z / 2) - 1) / z).mean(-1).real
-    c4 = dt * ((-4 - z + ez * (4 - 3 * z + z ** 2)) / z ** 3).mean(-1).real
-    c5 = dt * ((2 + z + ez * (-2 + z)) / z ** 3).mean(-1).real
-    c6 = dt * ((-4 - 3 * z - z ** 2 + ez * (4 - z)) / z ** 3).mean(-1).real
-    return E, E2, c1, c4, c5, c6
+
+    def mean(expr):
+        return dt * expr.mean(-1).real
+
+    out = {"E": E}
+    if scheme in (_lib.FSM_SETDRK1, _lib.FSM_SETDRK2):
+        out["c1"] = mean((ez - 1) / z)
+        if scheme == _lib.FSM_SETDRK2:
+            out["c2"] = mean((ez - 1 - z) / z ** 2)
+    elif scheme == _lib.FSM_SETDRK3:
+        out["E2"] = torch.exp(0.5 * dt * L)
+        out["c1"] = mean((torch.exp(z / 2) - 1) / z)
+        out["c2"] = mean((ez - 1) / z)
+        out["c3"] = mean((-4 - z + ez * (4 - 3 * z + z ** 2)) / z ** 3)
+        out["c4"] = mean((4.0 * (2.0 + z + ez * (-2 + z))) / z ** 3)
+        out["c5"] = mean((-4 - 3 * z - z ** 2 + ez * (4 - z)) / z ** 3)
+    elif scheme == _lib.FSM_SETDRK4:
+        out["E2"] = torch.exp(0.5 * dt * L)
+        out["c1"] = mean((torch.exp(z / 2) - 1) / z)
+        out["c4"] = mean((-4 - z + ez * (4 - 3 * z + z ** 2)) / z ** 3)
+        out["c5"] = mean((2 + z + ez * (-2 + z)) / z ** 3)
+        out["c6"] = mean((-4 - 3 * z - z ** 2 + ez * (4 - z)) / z ** 3)
+    else:
+        raise NotImplementedError(f"gradients: integrator code {scheme}")
+    return out
 
 
-def _setdrk4_step(u: torch.Tensor, tabs, nonlinear) -> torch.Tensor:
-    """One SETDRK4 step on full spectra in torch arithmetic (integrator/_stable_etdrk/_setdrk_step.py:55-82)."""
-    E, E2, c1, c4, c5, c6 = tabs
+def _scheme_step(scheme: int, u: torch.Tensor, T: dict, nonlinear, dt: float) -> torch.Tensor:
+    """One step of the scheme on full spectra in torch arithmetic: the stage recurrences of
+    integrator/_etdrk.py:22-82 (ETDRK0-2), _stable_etdrk/_setdrk_step.py:5-82 (SETDRK1-4) and the
+    fixed Runge-Kutta step of integrator/_rk.py:43-58 with its tableau."""
+    if scheme in _RK_TABLES:
+        L = T["L"]
+
+        def rhs(x):
+            return L * x if nonlinear is None else L * x + nonlinear(x)
+
+        rows, weights = _RK_TABLES[scheme]
+        ks = [rhs(u)]
+        for row in rows:
+            ks.append(rhs(u + dt * sum(a * k for a, k in zip(row[1:], ks))))
+        return u + dt * sum(w * k for w, k in zip(weights, ks))
+    E = T["E"]
+    if scheme == _lib.FSM_ETDRK0:
+        return E * u
+    if scheme in (_lib.FSM_ETDRK1, _lib.FSM_SETDRK1):
+        return E * u + T["c1"] * nonlinear(u)
+    if scheme in (_lib.FSM_ETDRK2, _lib.FSM_SETDRK2):
+        n0 = nonlinear(u)
+        a1 = E * u + T["c1"] * n0
+        return a1 + T["c2"] * (nonlinear(a1) - n0)
+    E2, c1 = T["E2"], T["c1"]
     n0 = nonlinear(u)
     a1 = E2 * u + c1 * n0
     n1 = nonlinear(a1)
+    if scheme == _lib.FSM_SETDRK3:
+        a2 = E * u + T["c2"] * (2 * n1 - n0)
+        n2 = nonlinear(a2)
+        return E * u + T["c3"] * n0 + T["c4"] * n1 + T["c5"] * n2
     a2 = E2 * u + c1 * n1
     n2 = nonlinear(a2)
     a3 = E2 * a1 + c1 * (2 * n2 - n0)
     n3 = nonlinear(a3)
-    return E * u + c4 * n0 + c5 * 2 * (n1 + n2) + c6 * n3
+    return E * u + T["c4"] * n0 + T["c5"] * 2 * (n1 + n2) + T["c6"] * n3
 
 
 class _RecomputeFn(torch.autograd.Function):
-    """Gradients of a SETDRK4 integration of any program (vorticity, KS, Leray, sources, complex
-    symbols, Python-callable terms): the forward runs the library's integration with checkpoints
-    every ``checkpoint`` steps; the backward recomputes each segment from its checkpoint with the
-    same step written in torch arithmetic on full spectra (the operator's own nonlinear closure, the
-    SETDRK4 tables from the FP64 contour formulas of the operator's linear symbol, rounded to FP32)
-    and differentiates that segment with torch autograd, last segment first. Only one segment's
-    graph is alive at a time."""
+    """Gradients of an integration of any program (vorticity, KS, Leray, sources, complex symbols,
+    Python-callable terms) under any fixed-step scheme (ETDRK0-2, SETDRK1-4, the Runge-Kutta
+    schemes): the forward runs the library's integration with checkpoints every ``checkpoint``
+    steps; the backward recomputes each segment from its checkpoint with the same step written in
+    torch arithmetic on full spectra (the operator's own nonlinear closure, the scheme's tables from
+    the FP64 formulas of the operator's linear symbol, rounded to FP32) and differentiates that
+    segment with torch autograd, last segment first. Only one segment's graph is alive at a time."""
 
     @staticmethod
-    def forward(ctx, u0, op, plan, spectral, dt, steps, checkpoint, *coefs):
+    def forward(ctx, u0, op, plan, spectral, dt, steps, checkpoint, scheme, *coefs):
         state = spectral.to_half(u0.detach()).contiguous()
         checkpoints = [state.clone()]
         done = 0
@@ -351,6 +413,7 @@ class _RecomputeFn(torch.autograd.Function):
             if done < steps:
                 checkpoints.append(state.clone())
         ctx.op, ctx.spectral, ctx.dt, ctx.steps, ctx.checkpoint = op, spectral, dt, steps, checkpoint
+        ctx.scheme = scheme
         ctx.checkpoints = checkpoints
         ctx.save_for_backward(u0, *coefs)
         return spectral.to_physical(state, keep_input=False)
@@ -372,7 +435,7 @@ class _RecomputeFn(torch.autograd.Function):
         r = float(cfg.get("integration_radius", 1.0))
         nonlinear = op._state_dict["nonlinear_func"]
         with torch.enable_grad():
-            leaves = [c.detach().requires_grad_(ctx.needs_input_grad[7 + i]) for i, c in enumerate(coefs)]
+            leaves = [c.detach().requires_grad_(ctx.needs_input_grad[8 + i]) for i, c in enumerate(coefs)]
             by_id = {id(c): leaf for c, leaf in zip(coefs, leaves)}
             L = None
             for coef, core in op._linear_terms:
@@ -384,8 +447,8 @@ class _RecomputeFn(torch.autograd.Function):
                 L = term if L is None else L + term
             if L is None:
                 L = torch.zeros((1, 1) + (1,) * nd, dtype=torch.complex128, device=u0.device)
-            tabs = [t.to(torch.complex64) if t.is_complex() else t.to(torch.float32)
-                    for t in _contour_tables_complex(L.to(torch.complex128), dt, M, r)]
+            tabs = {k: (t.to(torch.complex64) if t.is_complex() else t.to(torch.float32))
+                    for k, t in _scheme_tables(ctx.scheme, L.to(torch.complex128), dt, M, r).items()}
             v = grad_out.to(torch.float32)
             coef_grads = [None] * len(coefs)
             starts = list(range(0, steps, K))
@@ -399,7 +462,7 @@ class _RecomputeFn(torch.autograd.Function):
                     x_in = sp.half_to_full(ctx.checkpoints[si]).to(torch.complex64).detach().requires_grad_(True)
                     y = x_in
                 for _ in range(n):
-                    y = _setdrk4_step(y, tabs, nonlinear)
+                    y = _scheme_step(ctx.scheme, y, tabs, nonlinear, dt)
                 out = torch.fft.ifftn(y, dim=dims).real if si == len(starts) - 1 else y
                 wanted = [x_in] + [leaf for leaf in leaves if leaf.requires_grad]
                 grads = torch.autograd.grad(out, wanted, grad_outputs=v, allow_unused=True,
@@ -416,7 +479,7 @@ class _RecomputeFn(torch.autograd.Function):
                 else:
                     v = grads[0].detach()
         grads_out = [u0_grad.to(u0.dtype) if (u0_grad is not None and ctx.needs_input_grad[0]) else None]
-        grads_out += [None] * 6
+        grads_out += [None] * 7
         for i, c in enumerate(coefs):
             g = coef_grads[i]
             grads_out.append(g.to(c.dtype).reshape(c.shape) if g is not None else None)
@@ -448,13 +511,13 @@ def _prepare_and_apply(op, u0, dt, steps, checkpoint):
         op._build_integrator(dt, u0.device)
         integ = op._state_dict["integrator"]
     plan = integ.plan
-    if int(plan.integrator) != _lib.FSM_SETDRK4:
-        raise NotImplementedError("gradients are provided for the SETDRK4 integrator")
+    scheme = int(plan.integrator)
     coefs = [c for c, _ in op._linear_terms if isinstance(c, torch.Tensor) and c.requires_grad]
-    if not _convection_adjoint_applies(op, plan):
-        # any other program: segments recomputed and differentiated with torch autograd
+    if scheme != _lib.FSM_SETDRK4 or not _convection_adjoint_applies(op, plan):
+        # any other program or scheme: segments recomputed and differentiated with torch autograd
         with torch.enable_grad():
-            return _RecomputeFn.apply(u0, op, plan, integ.spectral, float(dt), int(steps), int(checkpoint), *coefs)
+            return _RecomputeFn.apply(u0, op, plan, integ.spectral, float(dt), int(steps), int(checkpoint), scheme,
+                                      *coefs)
     prog = plan.program
     L64 = op._linear_coef64(u0.device)
     h = plan.shape[-1] // 2 + 1

@@ -246,9 +246,10 @@ int fsm_adj_vjp_combine(int32_t batch_channels, int32_t nd, int64_t points, cons
  * (operator/_base.py:676-751) solves one batch at a time with one dt; each request here is
  * that solve with its own batch, step count and dt.
  *
- * fsm_serve_create: `plan` built with table_batch >= capacity (each slot has its own dt);
- *   `state` DEVICE complex64 [capacity][C][S]; `workspace` DEVICE of at least
- *   fsm_plan_workspace_bytes(plan, capacity, chunk) bytes; all work runs on `stream`. flags:
+ * fsm_serve_create: `plan` built with table_batch >= capacity (a table entry per request, each with
+ *   its own dt); `state` DEVICE complex64 [capacity][C][S]; `workspace` DEVICE of at least
+ *   fsm_serve_workspace_bytes(plan, capacity, chunk) bytes (the integration's workspace and the
+ *   slots' table entries); all work runs on `stream`. flags:
  *   FSM_SERVE_GRAPHS replays ticks of at most 64 steps as CUDA graphs (captured per
  *   (occupied slots, steps), step counts of such ticks rounded down to a power of two).
  *   tick_ms > 0 bounds a tick to about that much device time (from the measured time per step
@@ -259,7 +260,9 @@ int fsm_adj_vjp_combine(int32_t batch_channels, int32_t nd, int64_t points, cons
  *   out may be the same buffer). Both must stay valid until the request has left. Ids are the
  *   caller's and unique among pending requests.
  * fsm_serve_tick: if no tick is in flight, admit waiting requests in submission order while the
- *   head of the queue fits into the free slots, then launch k steps of every occupied slot
+ *   head of the queue fits into the free slots (each admitted request's coefficient tables are
+ *   computed once for its dt, in one table entry its samples share), then launch k steps of every
+ *   occupied slot
  *   (k = the fewest remaining steps, at most chunk and the tick_ms bound). *steps_launched = k,
  *   0 when a tick is in flight or no slot is occupied.
  * fsm_serve_poll: complete the tick in flight once the device has finished it (wait != 0:
@@ -284,6 +287,7 @@ typedef struct FsmServe FsmServe;
 #define FSM_SERVE_ACTIVE 1
 #define FSM_SERVE_DONE 2
 #define FSM_SERVE_NSTATS 10
+int fsm_serve_workspace_bytes(const FsmPlan* plan, int32_t capacity, int32_t chunk, size_t* bytes);
 int fsm_serve_create(FsmPlan* plan, int32_t capacity, int32_t chunk, void* state, void* workspace,
                      size_t workspace_bytes, int32_t flags, double tick_ms, void* stream, FsmServe** out);
 int fsm_serve_submit(FsmServe* server, int64_t request_id, int32_t batch, int32_t steps, double dt, const void* u0,

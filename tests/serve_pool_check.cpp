@@ -5,7 +5,8 @@
 // are applied as the engine applies them. Checks: occupied slots are always [0, occupied),
 // admission follows submission order without overtaking, every output receives its own
 // samples in order with exactly the requested steps, cancelled requests leave at the next
-// boundary with the steps they reached. Prints "ok" and exits 0, or names the failure.
+// boundary with the steps they reached, every active request holds one coefficient-table entry
+// of its own that all its slots map to. Prints "ok" and exits 0, or names the failure.
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -115,7 +116,10 @@ int main(int argc, char** argv) {
       leaving_total += (int)leaving.size();
       for (int32_t s = 0; s < cap; ++s)
         CHECK((slots[(size_t)s].id != -1) == (s < occ2), "after compaction slot %d vs %d occupied", s, occ2);
-      // every remaining active request's slots carry its own samples
+      // every remaining active request's slots carry its own samples, and map to its table entry
+      std::vector<int32_t> tabs((size_t)cap, -1);
+      pool.slot_tables(tabs.data());
+      std::map<int32_t, int64_t> entry_owner;
       for (int32_t s = 0; s < occ2; ++s) {
         int64_t id;
         int32_t index;
@@ -123,7 +127,14 @@ int main(int argc, char** argv) {
         CHECK(id == slots[(size_t)s].id && index == slots[(size_t)s].index, "slot %d owner mismatch", s);
         fsm::ServeRequest* r = pool.find(id);
         CHECK(r && r->slots[(size_t)index] == s, "request %lld does not list slot %d", (long long)id, s);
+        CHECK(r->tab >= 0 && r->tab < cap && tabs[(size_t)s] == r->tab, "slot %d table entry %d, request's %d", s,
+              tabs[(size_t)s], r->tab);
+        auto e = entry_owner.emplace(r->tab, id);
+        CHECK(e.first->second == id, "table entry %d held by requests %lld and %lld", r->tab,
+              (long long)e.first->second, (long long)id);
       }
+      CHECK((int32_t)entry_owner.size() + pool.free_tables() == cap, "table entries: %zu held + %d free != %d",
+            entry_owner.size(), pool.free_tables(), cap);
     }
     // outputs: own samples, in order, with the requested steps (or fewer when cancelled)
     for (const auto& kv : outputs) {

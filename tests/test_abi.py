@@ -72,6 +72,12 @@ def test_serving_engine_rejects_null_arguments_without_gpu(libpath):
     out = ctypes.c_void_p()
     assert lib.fsm_serve_create(None, 4, 8, None, None, 0, 0, 0.0, None, ctypes.byref(out)) == _lib.FSM_ERR_INVALID
     assert "serve_create" in _lib.last_error()
+    nb = ctypes.c_size_t()
+    assert lib.fsm_serve_workspace_bytes(None, 4, 8, ctypes.byref(nb)) == _lib.FSM_ERR_INVALID
+    grp = ctypes.c_void_p()
+    assert lib.fsm_serve_group_create(None, 2, 0.0, ctypes.byref(grp)) == _lib.FSM_ERR_INVALID
+    assert lib.fsm_serve_group_tick(None, ctypes.byref(k := ctypes.c_int32())) == _lib.FSM_ERR_INVALID
+    assert lib.fsm_serve_group_destroy(None) == _lib.FSM_OK
     assert lib.fsm_serve_submit(None, 1, 1, 1, 0.1, None, None) == _lib.FSM_ERR_INVALID
     k = ctypes.c_int32()
     assert lib.fsm_serve_tick(None, ctypes.byref(k)) == _lib.FSM_ERR_INVALID

@@ -78,6 +78,7 @@ EXPORTS = (
     "fsm_adj_vjp_combine",
     "fsm_step_adjoint_workspace_bytes",
     "fsm_step_adjoint",
+    "fsm_serve_workspace_bytes",
     "fsm_serve_create",
     "fsm_serve_submit",
     "fsm_serve_tick",
@@ -174,6 +175,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         lib.fsm_step_adjoint_workspace_bytes.argtypes = [vp, i32, ctypes.POINTER(sz)]
         lib.fsm_step_adjoint.argtypes = [vp, i32, vp, vp, vp, vp, vp, sz, vp]
         pi32, pi64 = ctypes.POINTER(i32), ctypes.POINTER(i64)
+        lib.fsm_serve_workspace_bytes.argtypes = [vp, i32, i32, ctypes.POINTER(sz)]
         lib.fsm_serve_create.argtypes = [vp, i32, i32, vp, vp, sz, i32, ctypes.c_double, vp, ctypes.POINTER(vp)]
         lib.fsm_serve_submit.argtypes = [vp, i64, i32, i32, ctypes.c_double, vp, vp]
         lib.fsm_serve_tick.argtypes = [vp, pi32]

@@ -322,8 +322,10 @@ class ServePool:
         self.handle = None
         with torch.cuda.stream(stream):
             self.state = torch.empty((self.capacity,) + self.sample_shape, dtype=torch.complex64, device=plan.device)
-            self.ws = torch.empty(plan.workspace_bytes(self.capacity, self.chunk), dtype=torch.uint8,
-                                  device=plan.device)
+            need = ctypes.c_size_t()
+            _lib.check(_lib.load().fsm_serve_workspace_bytes(plan.handle, self.capacity, self.chunk,
+                                                             ctypes.byref(need)))
+            self.ws = torch.empty(need.value, dtype=torch.uint8, device=plan.device)
         handle = ctypes.c_void_p()
         _lib.check(_lib.load().fsm_serve_create(
             plan.handle, self.capacity, self.chunk, self.state.data_ptr(), self.ws.data_ptr(), self.ws.numel(),

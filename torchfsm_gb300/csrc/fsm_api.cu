@@ -212,7 +212,7 @@ __global__ void k_pointwise(StepArgs a, int64_t total) {
     const int b = (int)(idx / (S * C));
     float2 u = a.state[idx];
     float2 aux[6] = {};  // scheme running sums (acc, q; Runge-Kutta partial inputs)
-    const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + s;
+    const int64_t toff = (tab_batch(a, b) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + s;
     const float2* tab = a.tab + toff;
     const float2 nv = a.src ? a.src[((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + s] : make_float2(0.f, 0.f);
     const int slot0 = a.slots ? a.slots[0] : -1;
@@ -733,7 +733,8 @@ StepArgs batch_arrays(const FsmPlan* p, StepArgs a, float2* arr, int b0, int n) 
   const int64_t per_sample = (int64_t)(p->n_aux * p->C + p->n_mid2) * S + (int64_t)(p->n_mid + p->n_prod) * p->ms;
   a.state += (int64_t)b0 * p->C * S;
   if (a.traj) a.traj += (int64_t)b0 * a.n_frames * p->C * S;
-  if (p->lin_batch > 1) a.tab += (int64_t)b0 * p->lin_ch * S;
+  if (a.tab_entry) a.tab_entry += b0;  // the samples' own entries
+  else if (p->lin_batch > 1) a.tab += (int64_t)b0 * p->lin_ch * S;
   if (a.src && p->src_batch > 1) a.src += (int64_t)b0 * p->C * S;
   a.aux = arr + (int64_t)b0 * per_sample;
   a.mid = a.aux + (int64_t)n * p->n_aux * p->C * S;
@@ -852,7 +853,7 @@ namespace {
 
 int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, const int32_t* record_slot, void* traj,
                    int32_t n_frames, void* workspace, size_t workspace_bytes, cudaStream_t st, LaunchProfile* prof,
-                   bool allow_split = true) {
+                   bool allow_split = true, const int32_t* tab_entry = nullptr) {
   if (!p || !state || batch < 1 || steps < 0) return set_error(FSM_ERR_INVALID, "integrate arguments");
   size_t off_arrays = 0;
   const size_t need = workspace_layout(p, batch, steps, &off_arrays);
@@ -889,6 +890,7 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
       return rc;
   }
   StepArgs a = base_args(p, state, batch, steps);
+  a.tab_entry = tab_entry;
   a.traj = (float2*)traj;
   a.n_frames = n_frames;
   a.slots = record_slot ? d_slots : nullptr;
@@ -952,8 +954,9 @@ int integrate_impl(const FsmPlan* p, int32_t batch, void* state, int32_t steps, 
 
 namespace fsm {
 int integrate_on_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
-                           size_t workspace_bytes, cudaStream_t st) {
-  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr, true);
+                           size_t workspace_bytes, cudaStream_t st, const int32_t* tab_entry) {
+  return integrate_impl(p, batch, state, steps, nullptr, nullptr, 0, workspace, workspace_bytes, st, nullptr, true,
+                        tab_entry);
 }
 
 int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,

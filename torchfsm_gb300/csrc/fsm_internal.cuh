@@ -45,7 +45,14 @@ struct StepArgs {
   const uint8_t* tile_zero;  // register axis-0 pass: column tiles whose next-stage fields are zero
   int hk;                     // 2D: last-axis columns of the stage fields stored and read (FsmPlan::hk)
   int64_t wp, ms;             // row pitch and field stride of mid / prod (FsmPlan::wp, ms)
+  const int32_t* tab_entry;   // per sample: its coefficient-table entry (serving), or null
 };
+
+// The coefficient-table entry of sample b: its own entry from tab_entry when given (a serving
+// engine's slots share their request's entry), else entry b of per-sample tables or the one entry.
+__device__ __forceinline__ int64_t tab_batch(const StepArgs& a, int b) {
+  return a.tab_entry ? (int64_t)a.tab_entry[b] : (int64_t)(a.lin_batch > 1 ? b : 0);
+}
 
 // The kernels' arguments for `batch` samples of `state` advanced by `steps` steps of plan p,
 // without recording (fsm_api.cu).
@@ -63,9 +70,10 @@ int integrate_with_workspace(const FsmPlan* p, int32_t batch, void* state, int32
                              size_t workspace_bytes, cudaStream_t st);
 size_t integrate_workspace_bytes(const FsmPlan* p, int32_t batch, int32_t steps);
 // fsm_integrate without recording on a caller-provided workspace; large batches may run in
-// parts on the library's streams (outside stream capture), as fsm_integrate does.
+// parts on the library's streams (outside stream capture), as fsm_integrate does. tab_entry
+// (device, one per sample, or null): each sample's coefficient-table entry.
 int integrate_on_workspace(const FsmPlan* p, int32_t batch, void* state, int32_t steps, void* workspace,
-                           size_t workspace_bytes, cudaStream_t st);
+                           size_t workspace_bytes, cudaStream_t st, const int32_t* tab_entry = nullptr);
 // Recompute the coefficient tables of batch entries [b0, b0 + n) for time step dt (one launch).
 int set_batch_dt_range(FsmPlan* p, int32_t b0, int32_t n, double dt, cudaStream_t st);
 

@@ -59,7 +59,7 @@ __device__ __forceinline__ void line_body(const StepArgs& a, int b, int t, const
   float2* q = acc + H;
   float2* gstate = a.state + (int64_t)b * H;
   for (int k = t; k < H; k += G) u[k] = gstate[k];
-  const int64_t toff = (int64_t)(a.lin_batch > 1 ? b : 0) * H;
+  const int64_t toff = tab_batch(a, b) * H;
   const float2* tab = a.tab + toff;
   const float2* src = a.src ? a.src + (int64_t)(a.src_batch > 1 ? b : 0) * H : nullptr;
   const int slot0 = a.slots ? a.slots[0] : -1;
@@ -214,7 +214,7 @@ __global__ void k_line_dc_fixup(StepArgs a) {
   const float2* mean = a.dc + (int64_t)a.steps * ns * a.B + a.B;
   float2 u = a.dc[(int64_t)a.steps * ns * a.B + b];
   float2 aux[6] = {};  // the scheme's running sums at k = 0
-  const float2* tab = a.tab + (int64_t)(a.lin_batch > 1 ? b : 0) * H;
+  const float2* tab = a.tab + tab_batch(a, b) * H;
   const float2 src0 = a.src ? a.src[(int64_t)(a.src_batch > 1 ? b : 0) * H] : make_float2(0.f, 0.f);
   for (int step = 0; step < a.steps; ++step) {
     for (int s = 0; s < ns; ++s) {

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_plane_col(StepArgs a) {
       } else {
         float2* accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
         float2* qp = a.aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
-        const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+        const int64_t toff = (tab_batch(a, b) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
         st[c] = etd_stage(a.integ, a.stage, nv[c], up, accp, qp, a.tab + toff, a.ts, (int64_t)C * S);
       }
       if (a.slot >= 0 && (a.stage < 0 || last))

@@ -158,7 +158,7 @@ __device__ __forceinline__ void axis0_update_hoisted(const StepArgs& a, float2* 
   float2* __restrict__ up = a.state + ((int64_t)b * C + c) * S + j;
   float2* __restrict__ accp = a.aux + ((int64_t)b * a.n_aux * C + c) * S + j;
   float2* __restrict__ qp = a.aux + ((int64_t)b * a.n_aux * C + C + c) * S + j;
-  const float2* __restrict__ tab = a.tab + ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + j;
+  const float2* __restrict__ tab = a.tab + (tab_batch(a, b) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + j;
   const float2* __restrict__ srcp =
       a.src ? a.src + ((int64_t)(a.src_batch > 1 ? b : 0) * C + c) * S + j : nullptr;
   const float2* __restrict__ o1p = (STG <= 1) ? up : accp;
@@ -253,7 +253,7 @@ __device__ __forceinline__ void axis0_update(const StepArgs& a, float2* __restri
       } else {
         float2* accp = aux + ((int64_t)b * a.n_aux * C + c) * S + sidx;
         float2* qp = aux + ((int64_t)b * a.n_aux * C + (a.n_aux > 1 ? C : 0) + c) * S + sidx;
-        const int64_t toff = ((int64_t)(a.lin_batch > 1 ? b : 0) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
+        const int64_t toff = (tab_batch(a, b) * a.lin_ch + (a.lin_ch > 1 ? c : 0)) * S + sidx;
         if (STG >= 0)
           st = etd_stage_c<INTEG, STG>(nv[f], up, accp, qp, tab + toff, a.ts);
         else

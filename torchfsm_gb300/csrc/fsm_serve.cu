@@ -35,7 +35,9 @@ struct FsmServe {
   int32_t chunk = 0;
   float2* state = nullptr;
   void* ws = nullptr;
-  size_t ws_bytes = 0;
+  size_t ws_bytes = 0;     // the integration's part of the workspace
+  int32_t* d_tabs = nullptr;  // the occupied slots' table entries (end of the workspace)
+  std::vector<int32_t> h_tabs;
   int32_t flags = 0;
   double tick_ms = 0.0;
   cudaStream_t st = nullptr;
@@ -93,10 +95,9 @@ int retire(FsmServe* s, const std::vector<fsm::ServeRequest*>& leaving) {
   int rc;
   for (const fsm::ServeRequest* r : leaving)
     if ((rc = copy_out(s, r))) return rc;
-  for (const fsm::SlotMove& m : s->pool.release(leaving)) {
+  // the slots' table entries follow their requests (slot_tables), so a move copies the state only
+  for (const fsm::SlotMove& m : s->pool.release(leaving))
     if ((rc = copy_slots(s, m.dst, 1, s->state + (int64_t)m.src * s->sample, true))) return rc;
-    if ((rc = fsm_plan_move_batch(s->plan, m.dst, m.src, s->st))) return rc;
-  }
   return FSM_OK;
 }
 
@@ -119,7 +120,7 @@ int advance(FsmServe* s, int32_t n, int32_t k, int64_t* launches) {
       cudaGraph_t g = nullptr;
       if ((rc = cuda_check(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal), "serve capture")))
         return rc;
-      const int irc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st);
+      const int irc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st, s->d_tabs);
       const cudaError_t ec = cudaStreamEndCapture(s->st, &g);
       if (irc) {
         if (g) cudaGraphDestroy(g);
@@ -146,7 +147,7 @@ int advance(FsmServe* s, int32_t n, int32_t k, int64_t* launches) {
     }
     s->seen.insert(key);
   }
-  if ((rc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st))) return rc;
+  if ((rc = fsm::integrate_on_workspace(s->plan, n, s->state, k, s->ws, s->ws_bytes, s->st, s->d_tabs))) return rc;
   return fsm_plan_launch_count(s->plan, n, k, launches);
 }
 
@@ -192,11 +193,21 @@ int finish_tick(FsmServe* s, bool wait) {
 int admit(FsmServe* s) {
   int rc;
   for (const fsm::ServeRequest* r : s->pool.admit()) {
-    const int32_t slot0 = r->slots.front();
-    if ((rc = copy_slots(s, slot0, r->batch, const_cast<void*>(r->u0), true))) return rc;
-    if ((rc = fsm::set_batch_dt_range(s->plan, slot0, r->batch, r->dt, s->st))) return rc;
+    if ((rc = copy_slots(s, r->slots.front(), r->batch, const_cast<void*>(r->u0), true))) return rc;
+    if ((rc = fsm::set_batch_dt_range(s->plan, r->tab, 1, r->dt, s->st))) return rc;  // its samples share it
   }
   return FSM_OK;
+}
+
+// The occupied slots' table entries to the device, before a tick's launches (outside any capture:
+// the captured ticks read them from d_tabs when they replay).
+int upload_tables(FsmServe* s) {
+  const int32_t n = s->pool.occupied();
+  if (n == 0) return FSM_OK;
+  s->pool.slot_tables(s->h_tabs.data());
+  return cuda_check(cudaMemcpyAsync(s->d_tabs, s->h_tabs.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                    s->st),
+                    "serve table entries");
 }
 
 // Round a graph-replayed tick's step count down to a power of two.
@@ -209,9 +220,26 @@ int32_t graph_steps(int32_t flags, int32_t k) {
   return k;
 }
 
+// The engine's workspace: the integration's workspace for (capacity, chunk), then the slots'
+// table entries (capacity int32, 256-byte aligned).
+int serve_layout(const FsmPlan* plan, int32_t capacity, int32_t chunk, size_t* tabs_off, size_t* total) {
+  size_t integ = 0;
+  int rc = fsm_plan_workspace_bytes(plan, capacity, chunk, &integ);
+  if (rc) return rc;
+  *tabs_off = (integ + 255) & ~(size_t)255;
+  *total = *tabs_off + (size_t)capacity * sizeof(int32_t);
+  return FSM_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int fsm_serve_workspace_bytes(const FsmPlan* plan, int32_t capacity, int32_t chunk, size_t* bytes) {
+  if (!plan || !bytes || capacity < 1 || chunk < 1) return set_error(FSM_ERR_INVALID, "serve_workspace_bytes arguments");
+  size_t off = 0;
+  return serve_layout(plan, capacity, chunk, &off, bytes);
+}
 
 int fsm_serve_create(FsmPlan* plan, int32_t capacity, int32_t chunk, void* state, void* workspace,
                      size_t workspace_bytes, int32_t flags, double tick_ms, void* stream, FsmServe** out) {
@@ -223,18 +251,21 @@ int fsm_serve_create(FsmPlan* plan, int32_t capacity, int32_t chunk, void* state
     return set_error(FSM_ERR_UNSUPPORTED, "serve_create: per-sample sources are not served");
   if (plan->nl == FSM_NL_KS && (plan->flags & FSM_FLAG_REMOVE_MEAN))
     return set_error(FSM_ERR_UNSUPPORTED, "serve_create: the batch-wide mean couples the samples");
-  size_t need = 0;
-  int rc = fsm_plan_workspace_bytes(plan, capacity, chunk, &need);
+  size_t need = 0, tabs_off = 0;
+  int rc = serve_layout(plan, capacity, chunk, &tabs_off, &need);
   if (rc) return rc;
   if (workspace_bytes < need)
-    return set_error(FSM_ERR_INVALID, "serve_create: workspace too small: need " + std::to_string(need) + " bytes");
+    return set_error(FSM_ERR_INVALID, "serve_create: workspace too small: need " + std::to_string(need) +
+                                          " bytes (fsm_serve_workspace_bytes)");
   FsmServe* s = new FsmServe(capacity);
   s->plan = plan;
   s->capacity = capacity;
   s->chunk = chunk;
   s->state = (float2*)state;
   s->ws = workspace;
-  s->ws_bytes = workspace_bytes;
+  s->ws_bytes = tabs_off;
+  s->d_tabs = (int32_t*)((char*)workspace + tabs_off);
+  s->h_tabs.assign((size_t)capacity, 0);
   s->flags = flags;
   s->tick_ms = tick_ms;
   s->st = (cudaStream_t)stream;
@@ -273,6 +304,7 @@ int fsm_serve_tick(FsmServe* s, int32_t* steps_launched) {
   if (s->step_ms > 0.0 && s->tick_ms > 0.0)
     limit = (int32_t)std::max(1.0, std::min(1e9, s->tick_ms / (s->step_ms * n)));
   const int32_t k = graph_steps(s->flags, s->pool.tick_steps(s->chunk, limit));
+  if ((rc = upload_tables(s))) return rc;
   if ((rc = cuda_check(cudaEventRecord(s->e0, s->st), "serve tick event"))) return rc;
   int64_t launched = 0;
   if ((rc = advance(s, n, k, &launched))) return rc;
@@ -410,6 +442,7 @@ int plane_tick(FsmServeGroup* g, int32_t k, int64_t* launched) {
     const int32_t n = s->pool.occupied();
     if (n == 0) continue;
     if ((rc = fsm::plane_args(s->plan, s->state, n, k, s->ws, s->ws_bytes, &pm.a[pm.count]))) return rc;
+    pm.a[pm.count].tab_entry = s->d_tabs;
     pm.n[pm.count] = s->plan->n[0];
     ++pm.count;
   }
@@ -496,6 +529,7 @@ int fsm_serve_group_tick(FsmServeGroup* g, int32_t* steps_launched) {
   int64_t total = 0;
   for (FsmServe* s : g->m) {
     if ((rc = admit(s))) return rc;
+    if ((rc = upload_tables(s))) return rc;
     total += s->pool.occupied();
   }
   if (total == 0) return FSM_OK;
@@ -514,6 +548,7 @@ int fsm_serve_group_tick(FsmServeGroup* g, int32_t* steps_launched) {
       const int32_t n = s->pool.occupied();
       if (n == 0) continue;
       lm.a[lm.count] = fsm::base_args(s->plan, s->state, n, k);
+      lm.a[lm.count].tab_entry = s->d_tabs;
       lm.n[lm.count] = s->plan->n[0];
       ++lm.count;
     }

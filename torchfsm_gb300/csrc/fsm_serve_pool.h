@@ -38,6 +38,7 @@ struct ServeRequest {
   int32_t status = kServeWaiting;
   bool cancel_pending = false;  // active request cancelled while a tick was in flight
   std::vector<int32_t> slots;   // slot of each sample while active
+  int32_t tab = -1;             // coefficient-table entry of the request's dt while active
 };
 
 struct SlotMove {
@@ -46,7 +47,10 @@ struct SlotMove {
 
 class SlotPool {
  public:
-  explicit SlotPool(int32_t capacity) : cap_(capacity), owner_((size_t)(capacity > 0 ? capacity : 0)) {}
+  explicit SlotPool(int32_t capacity) : cap_(capacity), owner_((size_t)(capacity > 0 ? capacity : 0)) {
+    // one coefficient-table entry per active request (its samples share its dt): at most one per slot
+    for (int32_t e = cap_ - 1; e >= 0; --e) free_tabs_.push_back(e);
+  }
 
   int32_t capacity() const { return cap_; }
   int32_t occupied() const { return occ_; }
@@ -76,6 +80,8 @@ class SlotPool {
       ServeRequest* r = queue_.front();
       queue_.pop_front();
       r->status = kServeActive;
+      r->tab = free_tabs_.back();  // never empty here: each active request holds a slot and at most one entry
+      free_tabs_.pop_back();
       r->slots.resize((size_t)r->batch);
       for (int32_t i = 0; i < r->batch; ++i) {
         r->slots[(size_t)i] = occ_ + i;
@@ -125,6 +131,8 @@ class SlotPool {
       for (int32_t s : r->slots) owner_[(size_t)s] = Owner{};
       occ_ -= r->batch;
       r->slots.clear();
+      free_tabs_.push_back(r->tab);
+      r->tab = -1;
       active_.erase(std::remove(active_.begin(), active_.end(), r), active_.end());
     }
     std::vector<SlotMove> moves;
@@ -142,6 +150,13 @@ class SlotPool {
     }
     return moves;
   }
+
+  // The table entry of each occupied slot [0, occupied) into out.
+  void slot_tables(int32_t* out) const {
+    for (int32_t s = 0; s < occ_; ++s) out[s] = owner_[(size_t)s].req ? owner_[(size_t)s].req->tab : 0;
+  }
+
+  int32_t free_tables() const { return (int32_t)free_tabs_.size(); }
 
   ServeRequest* find(int64_t id) const {
     auto it = reqs_.find(id);
@@ -179,6 +194,7 @@ class SlotPool {
   int32_t cap_;
   int32_t occ_ = 0;
   std::vector<Owner> owner_;
+  std::vector<int32_t> free_tabs_;  // coefficient-table entries not held by an active request
   std::deque<ServeRequest*> queue_;
   std::vector<ServeRequest*> active_;  // in admission order
   std::unordered_map<int64_t, std::unique_ptr<ServeRequest>> reqs_;

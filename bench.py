@@ -1344,7 +1344,7 @@ def main():
                     help="serving: the 1D KS buckets of every size advance together, one launch per tick")
     ap.add_argument("--group-planes", type=int, default=0,
                     help="serving: the 2D Burgers buckets of every size advance together, one launch per pass")
-    ap.add_argument("--priority", default="cheap", choices=["cheap", "costly"],
+    ap.add_argument("--priority", default="costly", choices=["cheap", "costly"],
                     help="serving: buckets on the high-priority streams")
     ap.add_argument("--workload", default="ns2d",
                     choices=["ns2d", "burgers1d", "burgers3d", "serving", "burgers2d_grad", "ks1d", "heat2d"],

@@ -126,14 +126,15 @@ int fsm_plan_create(const FsmMeshDesc* mesh, const FsmProgramDesc* program, doub
                     FsmPlan** out);
 
 /* Recompute the coefficient tables of batch entry b for time step dt
- * (plans with table_batch > 1). Mutates the plan: not to be called while
- * work using the plan is in flight on another stream. Used by the serving
- * loop to admit a request with its own dt into a slot. No counterpart in the
- * reference (its integrator holds one dt, integrator/_stable_etdrk/_uncached.py:180-211). */
+ * (plans with table_batch > 1): fsm_integrate then advances sample b with dt. Mutates the
+ * plan: not to be called while work using the plan is in flight on another stream. The
+ * serving engine does the same internally for each admitted request's table entry. No
+ * counterpart in the reference (its integrator holds one dt,
+ * integrator/_stable_etdrk/_uncached.py:180-211). */
 int fsm_plan_set_batch_dt(FsmPlan* plan, int32_t b, double dt, void* stream);
 
-/* Copy the coefficient tables of batch entry src to entry dst (slot
- * compaction in the serving loop). Same mutation rule as fsm_plan_set_batch_dt. */
+/* Copy the coefficient tables of batch entry src to entry dst (a caller that compacts its
+ * samples keeps each sample's dt). Same mutation rule as fsm_plan_set_batch_dt. */
 int fsm_plan_move_batch(FsmPlan* plan, int32_t dst, int32_t src, void* stream);
 
 /* Copy the plan's coefficient tables (complex64, [ntab][table_batch][lin_channel][S], the

@@ -612,9 +612,9 @@ def profile_kernels(plan, state0, ws, device) -> dict:
 
 
 # DRAM bytes of one column-pass launch at batch 64, from one ncu capture of `bench.py --ncu-case`
-# (dram__bytes_read.sum 36.5 MB + dram__bytes_write.sum 21.9 MB, stage 0 of a SETDRK4 step;
+# (dram__bytes_read.sum 35.8 MB + dram__bytes_write.sum 23.2 MB, stage 0 of a SETDRK4 step;
 # profiles/ns2d_vorticity_256x256_b64_plane_passes.md).
-COLUMN_PASS_DRAM_BYTES = 58.4e6
+COLUMN_PASS_DRAM_BYTES = 59.0e6
 
 
 HK = N // 3 + 1  # last-axis columns of the stage fields kept by the 2/3 rule (stored and read)

@@ -381,7 +381,8 @@ __device__ __forceinline__ void axis0_body(const StepArgs& a, int tile, int b) {
           // 0: psi = -w/lap, 1: i kx psi, 2: w, 3: i kx w
           if (mf < 2) {
             const float lap = -(kxv * kxv + gk.ky * gk.ky);
-            const float il = (lap == 0.f) ? 1.f : __fdividef(1.f, lap);  // |lap| <= 2 (NX/2)^2: within its range
+            // fast division: within 2 ulp for |lap| below 2^126, far above any mesh's 2 (pi NX / L)^2
+            const float il = (lap == 0.f) ? 1.f : __fdividef(1.f, lap);
             const float2 psi = cscale(d, -il);
             x = (mf == 0) ? psi : cscale(cmuli(psi), kxv);
           } else {

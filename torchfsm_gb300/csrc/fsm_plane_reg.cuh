@@ -474,7 +474,6 @@ template <int NY, int KIND, int HK>
 __device__ __forceinline__ void plane_row_body(const StepArgs& a, int blk, int b) {
   using Cfg = RowCfgR<NY>;
   constexpr int T = Cfg::T, E = Cfg::E, SCR = Cfg::SCR;
-  constexpr int H = NY / 2 + 1;
   extern __shared__ float2 smem[];
   float2* twt = smem;
   const int lane = threadIdx.x & 31;
